@@ -1,0 +1,201 @@
+/*
+ * regrid_gb300 — C ABI of the GB300 (sm_103a) regridding kernels.
+ *
+ * The upstream package (sun-data/regridding) is a Python + Numba library with
+ * no C interface; each entry point below replaces one of its compiled loops,
+ * cited beside it as upstream-path:line.  The Python package
+ * `regridding_gb300` binds these symbols with ctypes and keeps the upstream
+ * Python signatures on top.
+ *
+ * Conventions
+ *  - Every pointer argument named d_* is a device pointer on the current
+ *    device; h_* pointers are host memory.  Arrays are C-contiguous.
+ *  - Every function returns an RG_* status (0 = success).  On failure a
+ *    message is available from rg_last_error() in the calling thread.
+ *  - Work is enqueued on the given stream.  Functions that must return a
+ *    size to the host (the number of weights of a build) synchronise that
+ *    stream; this is stated beside them.  All others are asynchronous.
+ *  - Distinct handles may be used concurrently from different host threads
+ *    on different streams.  A handle must not be freed while work that uses
+ *    it is in flight.
+ *  - There is no CPU fallback: without a usable GPU every call fails with
+ *    RG_ERR_CUDA.
+ */
+#ifndef REGRID_GB300_H
+#define REGRID_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct CUstream_st* rg_stream_t; /* == cudaStream_t */
+
+/* status codes */
+#define RG_OK 0
+#define RG_ERR_ARG 1        /* invalid argument (the upstream raises ValueError) */
+#define RG_ERR_CUDA 2       /* CUDA runtime failure */
+#define RG_ERR_ALLOC 3      /* device allocation failed */
+#define RG_ERR_WALK 4       /* a sweep walk hit its step cap or was seated outside the grid */
+#define RG_ERR_UNSUPPORTED 5
+
+/* value dtypes */
+#define RG_F32 0
+#define RG_F64 1
+
+/* apply accumulation modes */
+#define RG_ACC_EXACT 0 /* double, multiply then add, entries in stored order: bit-identical to upstream */
+#define RG_ACC_FAST 1  /* accumulate in the output dtype with fused multiply-add */
+
+/* multilinear bounds (upstream `bounds` argument) */
+#define RG_BOUNDS_EXTRAPOLATE 0
+#define RG_BOUNDS_NAN 1
+#define RG_BOUNDS_RAISE 2
+
+typedef struct rg_weights_s* rg_weights; /* device-resident sparse weights of one element */
+
+/* Library version (major * 10000 + minor * 100 + patch). */
+int rg_version(void);
+
+/* Copies the calling thread's last error message into buf (always
+ * NUL-terminated); returns the message length. */
+int rg_last_error(char* buf, size_t n);
+
+/* ---------------------------------------------------------------- weights */
+
+/* Conservative (Ramshaw edge-sweep) weights between two logically
+ * rectangular 2D vertex grids of one orthogonal element.
+ * Replaces weights_conservative_2d,
+ *   regridding/_weights/_weights_conservative_2d/_weights_conservative_2d.py:76-126,
+ * together with the per-element coalescing of _coalesce,
+ *   regridding/_weights/_weights_arrays.py:44-73.
+ * Grids are (nx, ny) float64 arrays; d_w_in is NULL or (nxi-1, nyi-1).
+ * The output grid must already carry the upstream seeded perturbation if one
+ * is wanted (the host draws it).  Synchronises `stream` (twice: the raw and
+ * the merged entry counts size the buffers).  On success *out owns a new
+ * handle. */
+int rg_build_conservative_2d(const double* d_xi, const double* d_yi, int64_t nxi, int64_t nyi,
+                             const double* d_xo, const double* d_yo, int64_t nxo, int64_t nyo,
+                             const double* d_w_in, rg_stream_t stream, rg_weights* out);
+
+/* Weights from entries in the upstream saved layout (one element):
+ * indices_input, indices_output (int64, negative values count from the end as
+ * in numpy), values (float64).  Entries of one output are applied in the
+ * order given, as regridding/_regrid/_regrid_from_weights.py:179-182 does.
+ * Synchronises nothing. */
+int rg_weights_from_coo(const int64_t* d_in, const int64_t* d_out, const double* d_val, int64_t nnz,
+                        int64_t n_in, int64_t n_out, rg_stream_t stream, rg_weights* out);
+
+/* Number of stored entries and the matrix shape. */
+int rg_weights_info(rg_weights w, int64_t* nnz, int64_t* n_in, int64_t* n_out);
+
+/* Record the 2D shape of the output cells (rows of the matrix) so the apply
+ * can tile them in two dimensions.  Optional. */
+int rg_weights_set_output_shape(rg_weights w, int64_t n0, int64_t n1);
+
+/* Entries in the upstream saved layout: unique (input, output) pairs sorted by
+ * (input, output), as returned by regridding/_weights/_weights.py:186.
+ * Buffers hold nnz entries each. */
+int rg_weights_export_coo(rg_weights w, int64_t* d_in, int64_t* d_out, double* d_val,
+                          rg_stream_t stream);
+
+/* Free a handle (stream ordered on `stream`). */
+int rg_weights_free(rg_weights w, rg_stream_t stream);
+
+/* --------------------------------------------------------------- apply */
+
+/* values_output[d, o] = sum_k w[o,k] * values_input[d, col[o,k]] for d < stack.
+ * Replaces _regrid_from_weights, regridding/_regrid/_regrid_from_weights.py:165-182.
+ * d_vin is (stack, n_in) of dtype_in (RG_F32/RG_F64), d_vout is
+ * (stack, n_out) of dtype_out.  acc = RG_ACC_EXACT reproduces the upstream
+ * float64 result bit for bit (dtype_out must be RG_F64, or RG_F32 for the
+ * upstream in-place float32 output, which rounds after every update);
+ * RG_ACC_FAST accumulates in dtype_out with FMA. */
+int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dtype_out,
+             int64_t stack, int acc, rg_stream_t stream);
+
+/* The same with the transposed matrix (rows = input cells):
+ * values_input[d, i] = sum_o w[o, i] * values_output[d, o].  This is the
+ * apply of transpose_weights(),
+ * regridding/_weights/_weights_transposed/_weights_transposed.py:13-50, and
+ * the backward of the apply with respect to the values.  The first call
+ * builds the transposed index (stream ordered). */
+int rg_apply_transpose(rg_weights w, const void* d_vout, int dtype_out, void* d_vin, int dtype_in,
+                       int64_t stack, int acc, rg_stream_t stream);
+
+/* ------------------------------------------------------------ geometry */
+
+/* Cell areas of a 2D vertex grid: grid_volume,
+ * regridding/_weights/_weights_conservative_2d/_grids.py:50-140 (bit-identical). */
+int rg_cell_area_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, double* d_area,
+                    rg_stream_t stream);
+
+/* Cell lengths of a batch of 1D grids: cell_length,
+ * regridding/_weights/_weights_conservative_1d/_grids.py:10-35. d_x is (nd, n),
+ * d_len is (nd, n-1). */
+int rg_cell_length_1d(const double* d_x, int64_t nd, int64_t n, double* d_len, rg_stream_t stream);
+
+/* Locate points in a curvilinear 2D grid: the lowest-index cell containing
+ * each point, (INT64_MAX, INT64_MAX) outside.  method 0 = exhaustive order
+ * (index_of_point_brute, _grids.py:218-279); method 1 = the secant iteration
+ * with the local ascending search (index_of_point_secant, _grids.py:352-463);
+ * method 2 = grid walk (a new fast path with the exhaustive-order result on
+ * grids whose cells do not overlap). */
+int rg_locate_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, const double* d_px,
+                 const double* d_py, int64_t npts, int method, int64_t* d_i, int64_t* d_j,
+                 rg_stream_t stream);
+
+/* 1D find_indices on a batch of nd rows.  method 0 = brute
+ * (_find_indices_brute_1d, regridding/_find_indices/_find_indices_brute.py:24-51),
+ * method 1 = searchsorted (_find_indices_searchsorted_1d,
+ * regridding/_find_indices/_find_indices_searchsorted.py:24-62).  Row d of the
+ * inputs starts at d * x_stride (a stride of 0 broadcasts one row). */
+int rg_find_indices_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
+                       int64_t out_stride, int64_t n, int64_t nd, int method, int64_t fill_value,
+                       int64_t* d_result, rg_stream_t stream);
+
+/* Multilinear weights of nd 1D rows: find_indices(searchsorted), the bounds
+ * resolution of _weights_from_indices_multilinear
+ * (regridding/_weights/_weights_multilinear.py:101-119) and
+ * _weights_from_indices_multilinear_1d (:142-206), followed by the per-element
+ * coalescing (_coalesce).  Outputs are (nd, 2n) arrays in the upstream saved
+ * layout of each element.  With RG_BOUNDS_RAISE, *h_n_outside receives the
+ * number of outside points (synchronises) and nothing else is valid if it is
+ * nonzero.  d_w_in is NULL or rows of m values with stride w_stride.
+ * d_xout_search is NULL or the output coordinates used for the cell search
+ * (the upstream searches with the unperturbed coordinates and computes the
+ * weights from the perturbed ones when `perturb` is set); it shares
+ * out_stride with d_xout. */
+int rg_multilinear_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
+                      const double* d_xout_search, int64_t out_stride, int64_t n, int64_t nd,
+                      const double* d_w_in,
+                      int64_t w_stride, int bounds, int64_t* d_ind_in, int64_t* d_ind_out,
+                      double* d_val, int64_t* h_n_outside, rg_stream_t stream);
+
+/* Conservative 1D weights of nd rows: _weights_conservative_1d,
+ * regridding/_weights/_weights_conservative_1d/_weights_conservative_1d.py:59-318,
+ * followed by _coalesce.  Row d writes at most cap entries starting at
+ * d * cap; d_count[d] receives its entry count.  d_w_in is NULL or rows of
+ * m-1 values with stride w_stride. */
+int rg_conservative_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
+                       int64_t out_stride, int64_t n, int64_t nd, const double* d_w_in,
+                       int64_t w_stride, int64_t cap, int64_t* d_ind_in, int64_t* d_ind_out,
+                       double* d_val, int64_t* d_count, rg_stream_t stream);
+
+/* Conservative transpose scaling of entries in the saved layout:
+ * values * vol_in[i] / vol_out[o], first divided by w_in[i]^2 when d_w_in is
+ * not NULL.  Replaces the loop of transpose_weights_conservative,
+ * regridding/_weights/_weights_transposed/_weights_transposed.py:238-257.
+ * Indices may be negative (counted from the end). */
+int rg_transpose_conservative_scale(const int64_t* d_in, const int64_t* d_out, const double* d_val,
+                                    int64_t nnz, const double* d_vol_in, int64_t n_in,
+                                    const double* d_vol_out, int64_t n_out, const double* d_w_in,
+                                    double* d_result, rg_stream_t stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* REGRID_GB300_H */

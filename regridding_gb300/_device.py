@@ -1,0 +1,227 @@
+"""Device plumbing: torch CUDA buffers, the current stream, and device-resident weights.
+
+torch is used only to own device memory and to name the CUDA stream; every
+computation is a call into ``libregrid_gb300.so``.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import threading
+import weakref
+
+import numpy as np
+
+from . import _lib
+
+_torch = None
+
+
+def torch():
+    """Import torch lazily and require a CUDA device (no CPU fallback)."""
+    global _torch
+    if _torch is None:
+        import torch as t
+
+        _torch = t
+    if not _torch.cuda.is_available():
+        raise _lib.RegridError("regridding_gb300 needs a CUDA device; none is available")
+    return _torch
+
+
+def stream() -> ctypes.c_void_p:
+    return ctypes.c_void_p(torch().cuda.current_stream().cuda_stream)
+
+
+def ptr(t) -> ctypes.c_void_p | None:
+    return None if t is None else ctypes.c_void_p(t.data_ptr())
+
+
+def upload(a: np.ndarray, dtype=None):
+    """Host array -> contiguous CUDA tensor (pinned staging for large arrays)."""
+    t = torch()
+    a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
+    host = t.from_numpy(a) if a.dtype != np.bool_ else t.from_numpy(a.astype(np.uint8))
+    if a.nbytes >= (1 << 20):
+        host = host.pin_memory()
+        return host.to("cuda", non_blocking=True)
+    return host.to("cuda")
+
+
+def empty(shape, dtype):
+    t = torch()
+    return t.empty(shape, dtype=dtype, device="cuda")
+
+
+def download(t) -> np.ndarray:
+    return t.detach().cpu().numpy()
+
+
+_TORCH_DTYPES = {}
+
+
+def torch_dtype(np_dtype):
+    t = torch()
+    if not _TORCH_DTYPES:
+        _TORCH_DTYPES.update({np.dtype(np.float32): t.float32, np.dtype(np.float64): t.float64,
+                              np.dtype(np.int64): t.int64})
+    return _TORCH_DTYPES[np.dtype(np_dtype)]
+
+
+class DeviceWeights:
+    """Sparse weights of one orthogonal element, resident in GPU memory.
+
+    Rows are output cells and columns input cells.  Built by
+    :func:`build_conservative_2d`, :meth:`from_coo` or the public
+    :func:`regridding_gb300.weights`; applied with :meth:`apply`.
+    """
+
+    def __init__(self, handle: ctypes.c_void_p, shape_out: tuple[int, ...] | None = None):
+        self._h = handle
+        nnz, n_in, n_out = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
+        _lib.call("rg_weights_info", handle, ctypes.byref(nnz), ctypes.byref(n_in), ctypes.byref(n_out))
+        self.nnz, self.n_in, self.n_out = nnz.value, n_in.value, n_out.value
+        if shape_out is not None and len(shape_out) == 2 and shape_out[0] * shape_out[1] == self.n_out:
+            _lib.call("rg_weights_set_output_shape", handle, int(shape_out[0]), int(shape_out[1]))
+        self._finalizer = weakref.finalize(self, _free_handle, handle.value)
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    @classmethod
+    def from_coo(cls, indices_input, indices_output, values, n_in: int, n_out: int,
+                 shape_out: tuple[int, ...] | None = None) -> "DeviceWeights":
+        """Upload entries in the saved layout (numpy or CUDA tensors)."""
+        t = torch()
+        ii = _as_device(indices_input, t.int64)
+        oo = _as_device(indices_output, t.int64)
+        vv = _as_device(values, t.float64)
+        h = ctypes.c_void_p()
+        _lib.call("rg_weights_from_coo", ptr(ii), ptr(oo), ptr(vv), int(vv.numel()), int(n_in), int(n_out),
+                  stream(), ctypes.byref(h))
+        return cls(h, shape_out)
+
+    def export(self):
+        """Entries in the saved layout, sorted by (input, output), as CUDA tensors."""
+        t = torch()
+        ii = t.empty(self.nnz, dtype=t.int64, device="cuda")
+        oo = t.empty(self.nnz, dtype=t.int64, device="cuda")
+        vv = t.empty(self.nnz, dtype=t.float64, device="cuda")
+        _lib.call("rg_weights_export_coo", self._h, ptr(ii), ptr(oo), ptr(vv), stream())
+        return ii, oo, vv
+
+    def export_numpy(self):
+        ii, oo, vv = self.export()
+        return download(ii), download(oo), download(vv)
+
+    def apply(self, values, out=None, accumulate: str = "exact", transpose: bool = False):
+        """Apply to a CUDA tensor of shape (stack, n_in) (or (n_in,)).
+
+        ``accumulate="exact"`` reproduces the upstream float64 result bit for
+        bit (float64 output, or an upstream-style in-place float32 ``out``);
+        ``"fast"`` accumulates in the output dtype with FMA.
+        """
+        t = torch()
+        n_src, n_dst = (self.n_out, self.n_in) if transpose else (self.n_in, self.n_out)
+        squeeze = values.dim() == 1
+        v = values.reshape(-1, n_src)
+        if not v.is_contiguous():
+            v = v.contiguous()
+        if v.dtype not in (t.float32, t.float64):
+            v = v.to(t.float64)
+        stack = v.shape[0]
+        if out is None:
+            if accumulate == "exact":
+                odt = t.float64
+            else:
+                odt = v.dtype
+            out = t.empty((stack, n_dst), dtype=odt, device="cuda")
+        o = out.reshape(stack, n_dst)
+        acc = _lib.RG_ACC_EXACT if accumulate == "exact" else _lib.RG_ACC_FAST
+        dt_in = _lib.RG_F32 if v.dtype == t.float32 else _lib.RG_F64
+        dt_out = _lib.RG_F32 if o.dtype == t.float32 else _lib.RG_F64
+        fn = "rg_apply_transpose" if transpose else "rg_apply"
+        _lib.call(fn, self._h, ptr(v), dt_in, ptr(o), dt_out, int(stack), acc, stream())
+        return out.reshape(n_dst) if squeeze and out.dim() == 2 else out
+
+    def free(self) -> None:
+        self._finalizer()
+
+
+def _free_handle(h: int) -> None:
+    try:
+        lib = _lib.load(build_if_missing=False)
+        s = None
+        try:
+            import torch as t
+
+            if t.cuda.is_available():
+                s = ctypes.c_void_p(t.cuda.current_stream().cuda_stream)
+        except Exception:
+            s = None
+        lib.rg_weights_free(ctypes.c_void_p(h), s)
+    except Exception:
+        pass
+
+
+def _as_device(a, dtype):
+    t = torch()
+    if isinstance(a, t.Tensor):
+        return a.to(device="cuda", dtype=dtype).contiguous()
+    return upload(np.asarray(a), dtype={t.int64: np.int64, t.float64: np.float64}[dtype])
+
+
+def build_conservative_2d(grid_input, grid_output, weights_input=None) -> DeviceWeights:
+    """Conservative weights of one element from (x, y) vertex grids (numpy or CUDA tensors)."""
+    t = torch()
+    xi, yi = (_as_device(a, t.float64) for a in grid_input)
+    xo, yo = (_as_device(a, t.float64) for a in grid_output)
+    nxi, nyi = xi.shape
+    nxo, nyo = xo.shape
+    wi = None if weights_input is None else _as_device(weights_input, t.float64)
+    h = ctypes.c_void_p()
+    _lib.call("rg_build_conservative_2d", ptr(xi), ptr(yi), nxi, nyi, ptr(xo), ptr(yo), nxo, nyo, ptr(wi),
+              stream(), ctypes.byref(h))
+    return DeviceWeights(h, (nxo - 1, nyo - 1))
+
+
+# ---------------------------------------------------------------------------
+# device-resident copies of saved weights, keyed by the identity of their
+# (read-only) numpy arrays
+# ---------------------------------------------------------------------------
+
+_cache_lock = threading.Lock()
+_cache: dict[tuple, tuple] = {}
+
+
+def _drop(key: tuple) -> None:
+    with _cache_lock:
+        _cache.pop(key, None)
+
+
+def remember(element: tuple, dw: DeviceWeights) -> None:
+    """Associate the device copy with a saved-layout element whose arrays are read-only."""
+    ii, oo, vv = element
+    if not all(isinstance(a, np.ndarray) and not a.flags.writeable for a in (ii, oo, vv)):
+        return
+    key = (id(ii), id(oo), id(vv))
+    with _cache_lock:
+        _cache[key] = (weakref.ref(ii), weakref.ref(oo), weakref.ref(vv), dw)
+    weakref.finalize(vv, _drop, key)
+
+
+def lookup(element: tuple, n_in: int, n_out: int) -> DeviceWeights | None:
+    ii, oo, vv = element
+    if not isinstance(vv, np.ndarray):
+        return None
+    with _cache_lock:
+        hit = _cache.get((id(ii), id(oo), id(vv)))
+    if hit is None:
+        return None
+    ri, ro, rv, dw = hit
+    if ri() is not ii or ro() is not oo or rv() is not vv:
+        return None
+    if vv.flags.writeable or dw.n_in != n_in or dw.n_out != n_out:
+        return None
+    return dw

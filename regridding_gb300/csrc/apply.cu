@@ -1,0 +1,178 @@
+// Apply of device-resident weights to a stack of arrays:
+//   values_output[d, o] = sum_k w[o, k] * values_input[d, col[o, k]]
+// (regridding/_regrid/_regrid_from_weights.py:165-182).
+//
+// The matrix is stored by output row, so every output element is produced by
+// exactly one thread with no atomics.  A block covers a 2D tile of output
+// cells (8 x 32 when the output grid shape is known, so the input footprint of
+// the block is compact and its gathers reuse L1/L2 lines) and a chunk of the
+// stack; each thread keeps its row's first entries in registers and walks the
+// stack chunk, so the weights are read once per chunk instead of once per
+// array.
+#include "common.cuh"
+
+namespace rg {
+namespace {
+
+constexpr int APPLY_BLOCK = 256;
+constexpr int CACHED = 8;  // row entries held in registers
+
+template <typename T>
+__device__ __forceinline__ T ldg_cast(const T* p) { return __ldg(p); }
+
+struct Tile {
+    int64_t n0, n1;  // output shape used for tiling (n0 = 1 for 1D tiling)
+    int64_t tiles1;  // tiles along axis 1
+    int t0, t1;      // tile extent
+};
+
+__device__ __forceinline__ int64_t tile_row(const Tile& T, int64_t tile, int tid) {
+    int64_t ti = tile / T.tiles1, tj = tile % T.tiles1;
+    int64_t i = ti * T.t0 + tid / T.t1;
+    int64_t j = tj * T.t1 + tid % T.t1;
+    if (i >= T.n0 || j >= T.n1) return -1;
+    return i * T.n1 + j;
+}
+
+// MODE 0: exact double (mul then add, stored order), float64 output
+// MODE 1: exact double update rounded to float32 after every entry (numpy's
+//         in-place float32 output)
+// MODE 2: fast, accumulate in the output type with FMA
+template <typename Tin, typename Tout, int MODE, typename Tw>
+__global__ void __launch_bounds__(APPLY_BLOCK)
+    apply_kernel(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col,
+                 const Tw* __restrict__ val, Tile T, const Tin* __restrict__ vin, int64_t n_in,
+                 Tout* __restrict__ vout, int64_t n_out, int64_t stack, int64_t chunk) {
+    int64_t o = tile_row(T, blockIdx.x, threadIdx.x);
+    if (o < 0) return;
+    int64_t d0 = (int64_t)blockIdx.y * chunk;
+    int64_t d1 = d0 + chunk < stack ? d0 + chunk : stack;
+    int64_t s = row_ptr[o], e = row_ptr[o + 1];
+    int nk = (int)(e - s);
+    int32_t c[CACHED];
+    Tw w[CACHED];
+#pragma unroll
+    for (int k = 0; k < CACHED; k++) {
+        c[k] = k < nk ? col[s + k] : 0;
+        w[k] = k < nk ? val[s + k] : (Tw)0;
+    }
+    for (int64_t d = d0; d < d1; d++) {
+        const Tin* a = vin + d * n_in;
+        if (MODE == 0) {
+            double acc = 0.0;
+#pragma unroll
+            for (int k = 0; k < CACHED; k++)
+                if (k < nk) acc = __dadd_rn(acc, __dmul_rn((double)w[k], (double)ldg_cast(a + c[k])));
+            for (int64_t k = s + CACHED; k < e; k++)
+                acc = __dadd_rn(acc, __dmul_rn((double)val[k], (double)ldg_cast(a + col[k])));
+            vout[d * n_out + o] = (Tout)acc;
+        } else if (MODE == 1) {
+            float acc = 0.0f;
+#pragma unroll
+            for (int k = 0; k < CACHED; k++)
+                if (k < nk)
+                    acc = (float)__dadd_rn((double)acc, __dmul_rn((double)w[k], (double)ldg_cast(a + c[k])));
+            for (int64_t k = s + CACHED; k < e; k++)
+                acc = (float)__dadd_rn((double)acc, __dmul_rn((double)val[k], (double)ldg_cast(a + col[k])));
+            vout[d * n_out + o] = (Tout)acc;
+        } else {
+            Tout acc = (Tout)0;
+#pragma unroll
+            for (int k = 0; k < CACHED; k++)
+                if (k < nk) acc = fma((Tout)w[k], (Tout)ldg_cast(a + c[k]), acc);
+            for (int64_t k = s + CACHED; k < e; k++) acc = fma((Tout)val[k], (Tout)ldg_cast(a + col[k]), acc);
+            vout[d * n_out + o] = acc;
+        }
+    }
+}
+
+__global__ void to_f32(const double* a, float* b, int64_t n) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        b[k] = (float)a[k];
+}
+
+template <typename Tin, typename Tout, int MODE, typename Tw>
+int launch(const int64_t* row_ptr, const int32_t* col, const Tw* val, int64_t n_rows,
+           int64_t shape0, int64_t shape1, const void* vin, int64_t n_in, void* vout, int64_t stack,
+           cudaStream_t s) {
+    Tile T;
+    if (shape0 > 0 && shape1 > 0 && shape0 * shape1 == n_rows && shape1 >= 32) {
+        T.n0 = shape0;
+        T.n1 = shape1;
+        T.t0 = 8;
+        T.t1 = 32;
+    } else {
+        T.n0 = 1;
+        T.n1 = n_rows;
+        T.t0 = 1;
+        T.t1 = APPLY_BLOCK;
+    }
+    T.tiles1 = (T.n1 + T.t1 - 1) / T.t1;
+    int64_t tiles = ((T.n0 + T.t0 - 1) / T.t0) * T.tiles1;
+    // stack chunk: enough blocks to fill the GPU, at most 65535 along y
+    int64_t chunk = 16;
+    if (tiles >= 4 * 152 * 8) chunk = 64;
+    if ((stack + chunk - 1) / chunk > 65535) chunk = (stack + 65534) / 65535;
+    int64_t chunks = (stack + chunk - 1) / chunk;
+    RG_CHECK(tiles < 0x7fffffff, RG_ERR_UNSUPPORTED, "apply: too many output cells");
+    dim3 grid((unsigned)tiles, (unsigned)chunks);
+    apply_kernel<Tin, Tout, MODE, Tw><<<grid, APPLY_BLOCK, 0, s>>>(
+        row_ptr, col, val, T, (const Tin*)vin, n_in, (Tout*)vout, n_rows, stack, chunk);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, float** val32,
+              int64_t nnz, int64_t n_rows, int64_t n_cols, int64_t shape0, int64_t shape1,
+              const void* vin, int dtype_in, void* vout, int dtype_out, int64_t stack, int acc,
+              cudaStream_t s) {
+    RG_CHECK(dtype_in == RG_F32 || dtype_in == RG_F64, RG_ERR_ARG, "apply: bad input dtype");
+    RG_CHECK(dtype_out == RG_F32 || dtype_out == RG_F64, RG_ERR_ARG, "apply: bad output dtype");
+    RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST, RG_ERR_ARG, "apply: bad accumulation mode");
+    if (stack <= 0 || n_rows <= 0) return RG_OK;
+    if (acc == RG_ACC_EXACT) {
+        if (dtype_out == RG_F64) {
+            if (dtype_in == RG_F32)
+                return launch<float, double, 0, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols,
+                                                        vout, stack, s);
+            return launch<double, double, 0, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols,
+                                                     vout, stack, s);
+        }
+        if (dtype_in == RG_F32)
+            return launch<float, float, 1, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols, vout,
+                                                   stack, s);
+        return launch<double, float, 1, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols, vout,
+                                                stack, s);
+    }
+    if (dtype_out == RG_F64) {
+        if (dtype_in == RG_F32)
+            return launch<float, double, 2, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols, vout,
+                                                    stack, s);
+        return launch<double, double, 2, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols, vout,
+                                                 stack, s);
+    }
+    // float32 output, fast: weights rounded to float once (lazily cached)
+    if (*val32 == nullptr && nnz > 0) {
+        RG_TRY(dalloc(val32, (size_t)nnz, s));
+        to_f32<<<grid_for(nnz, 256) > 8192 ? 8192 : grid_for(nnz, 256), 256, 0, s>>>(val, *val32, nnz);
+    }
+    if (dtype_in == RG_F32)
+        return launch<float, float, 2, float>(row_ptr, col, *val32, n_rows, shape0, shape1, vin, n_cols, vout,
+                                              stack, s);
+    return launch<double, float, 2, float>(row_ptr, col, *val32, n_rows, shape0, shape1, vin, n_cols, vout,
+                                           stack, s);
+}
+
+}  // namespace
+
+int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_in, void* vout,
+                  int dtype_out, int64_t stack, int acc, cudaStream_t s) {
+    if (!transposed)
+        return apply_csr(W->row_ptr, W->col, W->val, &W->val32, W->nnz, W->n_out, W->n_in, W->out_shape0,
+                         W->out_shape1, vin, dtype_in, vout, dtype_out, stack, acc, s);
+    return apply_csr(W->t_row_ptr, W->t_col, W->t_val, &W->t_val32, W->nnz, W->n_in, W->n_out, 0, 0, vin,
+                     dtype_in, vout, dtype_out, stack, acc, s);
+}
+
+}  // namespace rg

@@ -1,0 +1,384 @@
+// extern "C" entry points of libregrid_gb300 (declared in include/regrid_gb300.h).
+#include <cstdarg>
+#include <cstring>
+#include <new>
+
+#include "common.cuh"
+
+namespace rg {
+
+static thread_local char g_err[1024] = {0};
+
+void set_error(const char* fmt, ...) {
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+const char* last_error() { return g_err; }
+
+// implemented in the kernel files
+int build_conservative_2d(const double*, const double*, int64_t, int64_t, const double*, const double*,
+                          int64_t, int64_t, const double*, cudaStream_t, rg_weights_s*);
+int cell_area_2d(const double*, const double*, int64_t, int64_t, double*, cudaStream_t);
+int locate_2d_exact(const double*, const double*, int64_t, int64_t, const double*, const double*, int64_t,
+                    int, int64_t*, int64_t*, cudaStream_t);
+int locate_2d_walk(const double*, const double*, int64_t, int64_t, const double*, const double*, int64_t,
+                   int64_t*, int64_t*, cudaStream_t);
+int apply_weights(rg_weights_s*, bool, const void*, int, void*, int, int64_t, int, cudaStream_t);
+int find_indices_1d(const double*, int64_t, int64_t, const double*, int64_t, int64_t, int64_t, int, int64_t,
+                    int64_t*, cudaStream_t);
+int multilinear_1d(const double*, int64_t, int64_t, const double*, const double*, int64_t, int64_t, int64_t,
+                   const double*, int64_t, int, int64_t*, int64_t*, double*, int64_t*, cudaStream_t);
+int conservative_1d(const double*, int64_t, int64_t, const double*, int64_t, int64_t, int64_t, const double*,
+                    int64_t, int64_t, int64_t*, int64_t*, double*, int64_t*, cudaStream_t);
+int cell_length_1d(const double*, int64_t, int64_t, double*, cudaStream_t);
+int transpose_conservative_scale(const int64_t*, const int64_t*, const double*, int64_t, const double*,
+                                 int64_t, const double*, int64_t, const double*, double*, cudaStream_t);
+
+namespace {
+
+// entries of a COO list normalised to [0, n) (numpy-style negative indices)
+__global__ void normalise_coo(const int64_t* in, const int64_t* out, int64_t nnz, int64_t n_in,
+                              int64_t n_out, int32_t* in32, int32_t* out32, int64_t* pos,
+                              unsigned* bad) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int64_t i = in[k], o = out[k];
+        if (i < 0) i += n_in;
+        if (o < 0) o += n_out;
+        if (i < 0 || i >= n_in || o < 0 || o >= n_out) {
+            atomicOr(bad, 1u);
+            i = 0;
+            o = 0;
+        }
+        in32[k] = (int32_t)i;
+        out32[k] = (int32_t)o;
+        pos[k] = k;
+    }
+}
+
+__global__ void gather_csr(const uint32_t* perm, const int32_t* in32, const double* val, int64_t nnz,
+                           int32_t* col, double* cval) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t e = perm[k];
+        col[k] = in32[e];
+        cval[k] = val[e];
+    }
+}
+
+// row index of every stored entry, and the key (row, position) that orders
+// entries of equal column by row
+__global__ void expand_rows(const int64_t* row_ptr, int64_t n_rows, int32_t* row_of, int64_t* key) {
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n_rows;
+         r += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t k = row_ptr[r]; k < row_ptr[r + 1]; k++) {
+            row_of[k] = (int32_t)r;
+            key[k] = ((int64_t)r << 32) | (int64_t)(uint32_t)k;
+        }
+    }
+}
+
+__global__ void gather_transposed(const uint32_t* perm, const int32_t* row_of, const double* val,
+                                  int64_t nnz, int32_t* t_col, double* t_val) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t e = perm[k];
+        t_col[k] = row_of[e];
+        t_val[k] = val[e];
+    }
+}
+
+__global__ void gather_export(const uint32_t* perm, const int32_t* col, const int32_t* row_of,
+                              const double* val, int64_t nnz, int64_t* e_in, int64_t* e_out,
+                              double* e_val) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nnz;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        uint32_t e = perm[k];
+        e_in[k] = col[e];
+        e_out[k] = row_of[e];
+        e_val[k] = val[e];
+    }
+}
+
+inline unsigned capped(int64_t n, int block, unsigned cap = 65536) {
+    unsigned g = grid_for(n, block);
+    return g > cap ? cap : g;
+}
+
+// Column-major order of the stored entries: perm over CSR positions sorted
+// by (column, row), plus the row of every entry.
+int column_order(rg_weights_s* W, int32_t** row_of, uint32_t** perm, int64_t** col_ptr,
+                 cudaStream_t s) {
+    int64_t* key = nullptr;
+    int st = RG_OK;
+    *row_of = nullptr;
+    *perm = nullptr;
+    *col_ptr = nullptr;
+    do {
+        if ((st = dalloc(row_of, (size_t)W->nnz, s))) break;
+        if ((st = dalloc(&key, (size_t)W->nnz, s))) break;
+        if ((st = dalloc(perm, (size_t)W->nnz, s))) break;
+        if ((st = dalloc(col_ptr, (size_t)W->n_in + 1, s))) break;
+        expand_rows<<<capped(W->n_out, 128), 128, 0, s>>>(W->row_ptr, W->n_out, *row_of, key);
+        st = bucket_sort(W->col, key, W->nnz, W->n_in, *col_ptr, *perm, nullptr, s);
+    } while (0);
+    dfree(key, s);
+    if (st) {
+        dfree(*row_of, s);
+        dfree(*perm, s);
+        dfree(*col_ptr, s);
+        *row_of = nullptr;
+        *perm = nullptr;
+        *col_ptr = nullptr;
+    }
+    return st;
+}
+
+int ensure_transposed(rg_weights_s* W, cudaStream_t s) {
+    if (W->t_row_ptr) return RG_OK;
+    int32_t* row_of = nullptr;
+    uint32_t* perm = nullptr;
+    int64_t* col_ptr = nullptr;
+    RG_TRY(column_order(W, &row_of, &perm, &col_ptr, s));
+    int st = RG_OK;
+    do {
+        if ((st = dalloc(&W->t_col, (size_t)W->nnz, s))) break;
+        if ((st = dalloc(&W->t_val, (size_t)W->nnz, s))) break;
+        if (W->nnz > 0)
+            gather_transposed<<<capped(W->nnz, 256), 256, 0, s>>>(perm, row_of, W->val, W->nnz, W->t_col,
+                                                                 W->t_val);
+        W->t_row_ptr = col_ptr;
+        col_ptr = nullptr;
+        cudaError_t e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("transpose: %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+        }
+    } while (0);
+    dfree(row_of, s);
+    dfree(perm, s);
+    dfree(col_ptr, s);
+    return st;
+}
+
+void free_weights(rg_weights_s* W, cudaStream_t s) {
+    dfree(W->row_ptr, s);
+    dfree(W->col, s);
+    dfree(W->val, s);
+    dfree(W->val32, s);
+    dfree(W->t_row_ptr, s);
+    dfree(W->t_col, s);
+    dfree(W->t_val, s);
+    dfree(W->t_val32, s);
+    delete W;
+}
+
+}  // namespace
+}  // namespace rg
+
+using namespace rg;
+
+extern "C" {
+
+int rg_version(void) { return 100; }
+
+int rg_last_error(char* buf, size_t n) {
+    size_t len = strlen(g_err);
+    if (buf && n) {
+        size_t c = len < n - 1 ? len : n - 1;
+        memcpy(buf, g_err, c);
+        buf[c] = 0;
+    }
+    return (int)len;
+}
+
+int rg_build_conservative_2d(const double* d_xi, const double* d_yi, int64_t nxi, int64_t nyi,
+                             const double* d_xo, const double* d_yo, int64_t nxo, int64_t nyo,
+                             const double* d_w_in, rg_stream_t stream, rg_weights* out) {
+    RG_CHECK(out, RG_ERR_ARG, "rg_build_conservative_2d: out is NULL");
+    *out = nullptr;
+    rg_weights_s* W = new (std::nothrow) rg_weights_s();
+    RG_CHECK(W, RG_ERR_ALLOC, "host allocation failed");
+    cudaGetDevice(&W->device);
+    int st = build_conservative_2d(d_xi, d_yi, nxi, nyi, d_xo, d_yo, nxo, nyo, d_w_in,
+                                   (cudaStream_t)stream, W);
+    if (st) {
+        free_weights(W, (cudaStream_t)stream);
+        return st;
+    }
+    *out = W;
+    return RG_OK;
+}
+
+int rg_weights_from_coo(const int64_t* d_in, const int64_t* d_out, const double* d_val, int64_t nnz,
+                        int64_t n_in, int64_t n_out, rg_stream_t stream, rg_weights* out) {
+    RG_CHECK(out, RG_ERR_ARG, "rg_weights_from_coo: out is NULL");
+    RG_CHECK(nnz >= 0 && n_in >= 0 && n_out >= 0, RG_ERR_ARG, "rg_weights_from_coo: negative size");
+    RG_CHECK(n_in < INT32_MAX && n_out < INT32_MAX, RG_ERR_UNSUPPORTED,
+             "rg_weights_from_coo: more than 2^31 cells");
+    *out = nullptr;
+    cudaStream_t s = (cudaStream_t)stream;
+    rg_weights_s* W = new (std::nothrow) rg_weights_s();
+    RG_CHECK(W, RG_ERR_ALLOC, "host allocation failed");
+    cudaGetDevice(&W->device);
+    W->n_in = n_in;
+    W->n_out = n_out;
+    W->nnz = nnz;
+    int32_t *in32 = nullptr, *out32 = nullptr;
+    int64_t* pos = nullptr;
+    uint32_t* perm = nullptr;
+    unsigned* bad = nullptr;
+    int st = RG_OK;
+    do {
+        if ((st = dalloc(&in32, (size_t)nnz, s))) break;
+        if ((st = dalloc(&out32, (size_t)nnz, s))) break;
+        if ((st = dalloc(&pos, (size_t)nnz, s))) break;
+        if ((st = dalloc(&perm, (size_t)nnz, s))) break;
+        if ((st = dalloc(&bad, 1, s))) break;
+        if ((st = dalloc(&W->row_ptr, (size_t)n_out + 1, s))) break;
+        if ((st = dalloc(&W->col, (size_t)nnz, s))) break;
+        if ((st = dalloc(&W->val, (size_t)nnz, s))) break;
+        cudaMemsetAsync(bad, 0, sizeof(unsigned), s);
+        if (nnz > 0)
+            normalise_coo<<<capped(nnz, 256), 256, 0, s>>>(d_in, d_out, nnz, n_in, n_out, in32, out32, pos,
+                                                          bad);
+        if (n_out > 0) {
+            if ((st = bucket_sort(out32, pos, nnz, n_out, W->row_ptr, perm, nullptr, s))) break;
+        } else {
+            cudaMemsetAsync(W->row_ptr, 0, sizeof(int64_t), s);
+        }
+        if (nnz > 0) gather_csr<<<capped(nnz, 256), 256, 0, s>>>(perm, in32, d_val, nnz, W->col, W->val);
+        unsigned hbad = 0;
+        cudaMemcpyAsync(&hbad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("rg_weights_from_coo: %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        if (hbad) {
+            set_error("rg_weights_from_coo: an index is out of range for the given shapes");
+            st = RG_ERR_ARG;
+        }
+    } while (0);
+    dfree(in32, s);
+    dfree(out32, s);
+    dfree(pos, s);
+    dfree(perm, s);
+    dfree(bad, s);
+    if (st) {
+        free_weights(W, s);
+        return st;
+    }
+    *out = W;
+    return RG_OK;
+}
+
+int rg_weights_info(rg_weights w, int64_t* nnz, int64_t* n_in, int64_t* n_out) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_weights_info: NULL handle");
+    if (nnz) *nnz = w->nnz;
+    if (n_in) *n_in = w->n_in;
+    if (n_out) *n_out = w->n_out;
+    return RG_OK;
+}
+
+int rg_weights_set_output_shape(rg_weights w, int64_t n0, int64_t n1) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_weights_set_output_shape: NULL handle");
+    RG_CHECK(n0 * n1 == w->n_out, RG_ERR_ARG, "rg_weights_set_output_shape: %lld x %lld != %lld",
+             (long long)n0, (long long)n1, (long long)w->n_out);
+    w->out_shape0 = n0;
+    w->out_shape1 = n1;
+    return RG_OK;
+}
+
+int rg_weights_export_coo(rg_weights w, int64_t* d_in, int64_t* d_out, double* d_val,
+                          rg_stream_t stream) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_weights_export_coo: NULL handle");
+    if (w->nnz == 0) return RG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    int32_t* row_of = nullptr;
+    uint32_t* perm = nullptr;
+    int64_t* col_ptr = nullptr;
+    RG_TRY(column_order(w, &row_of, &perm, &col_ptr, s));
+    gather_export<<<capped(w->nnz, 256), 256, 0, s>>>(perm, w->col, row_of, w->val, w->nnz, d_in, d_out,
+                                                     d_val);
+    dfree(row_of, s);
+    dfree(perm, s);
+    dfree(col_ptr, s);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+int rg_weights_free(rg_weights w, rg_stream_t stream) {
+    if (w) free_weights(w, (cudaStream_t)stream);
+    return RG_OK;
+}
+
+int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dtype_out, int64_t stack,
+             int acc, rg_stream_t stream) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_apply: NULL handle");
+    return apply_weights(w, false, d_vin, dtype_in, d_vout, dtype_out, stack, acc, (cudaStream_t)stream);
+}
+
+int rg_apply_transpose(rg_weights w, const void* d_vout, int dtype_out, void* d_vin, int dtype_in,
+                       int64_t stack, int acc, rg_stream_t stream) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_apply_transpose: NULL handle");
+    RG_TRY(ensure_transposed(w, (cudaStream_t)stream));
+    return apply_weights(w, true, d_vout, dtype_out, d_vin, dtype_in, stack, acc, (cudaStream_t)stream);
+}
+
+int rg_cell_area_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, double* d_area,
+                    rg_stream_t stream) {
+    RG_CHECK(nx >= 2 && ny >= 2, RG_ERR_ARG, "rg_cell_area_2d: need at least 2x2 vertices");
+    return cell_area_2d(d_x, d_y, nx, ny, d_area, (cudaStream_t)stream);
+}
+
+int rg_cell_length_1d(const double* d_x, int64_t nd, int64_t n, double* d_len, rg_stream_t stream) {
+    RG_CHECK(n >= 1, RG_ERR_ARG, "rg_cell_length_1d: empty grid");
+    return cell_length_1d(d_x, nd, n, d_len, (cudaStream_t)stream);
+}
+
+int rg_locate_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, const double* d_px,
+                 const double* d_py, int64_t npts, int method, int64_t* d_i, int64_t* d_j,
+                 rg_stream_t stream) {
+    RG_CHECK(nx >= 2 && ny >= 2, RG_ERR_ARG, "rg_locate_2d: need at least 2x2 vertices");
+    RG_CHECK(method >= 0 && method <= 2, RG_ERR_ARG, "rg_locate_2d: unknown method %d", method);
+    if (method == 2)
+        return locate_2d_walk(d_x, d_y, nx, ny, d_px, d_py, npts, d_i, d_j, (cudaStream_t)stream);
+    return locate_2d_exact(d_x, d_y, nx, ny, d_px, d_py, npts, method, d_i, d_j, (cudaStream_t)stream);
+}
+
+int rg_find_indices_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
+                       int64_t out_stride, int64_t n, int64_t nd, int method, int64_t fill_value,
+                       int64_t* d_result, rg_stream_t stream) {
+    return find_indices_1d(d_xin, in_stride, m, d_xout, out_stride, n, nd, method, fill_value, d_result,
+                           (cudaStream_t)stream);
+}
+
+int rg_multilinear_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
+                      const double* d_xout_search, int64_t out_stride, int64_t n, int64_t nd,
+                      const double* d_w_in, int64_t w_stride, int bounds, int64_t* d_ind_in,
+                      int64_t* d_ind_out, double* d_val, int64_t* h_n_outside, rg_stream_t stream) {
+    return multilinear_1d(d_xin, in_stride, m, d_xout, d_xout_search, out_stride, n, nd, d_w_in, w_stride,
+                          bounds, d_ind_in, d_ind_out, d_val, h_n_outside, (cudaStream_t)stream);
+}
+
+int rg_conservative_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
+                       int64_t out_stride, int64_t n, int64_t nd, const double* d_w_in, int64_t w_stride,
+                       int64_t cap, int64_t* d_ind_in, int64_t* d_ind_out, double* d_val, int64_t* d_count,
+                       rg_stream_t stream) {
+    return conservative_1d(d_xin, in_stride, m, d_xout, out_stride, n, nd, d_w_in, w_stride, cap, d_ind_in,
+                           d_ind_out, d_val, d_count, (cudaStream_t)stream);
+}
+
+int rg_transpose_conservative_scale(const int64_t* d_in, const int64_t* d_out, const double* d_val,
+                                    int64_t nnz, const double* d_vol_in, int64_t n_in,
+                                    const double* d_vol_out, int64_t n_out, const double* d_w_in,
+                                    double* d_result, rg_stream_t stream) {
+    return transpose_conservative_scale(d_in, d_out, d_val, nnz, d_vol_in, n_in, d_vol_out, n_out, d_w_in,
+                                        d_result, (cudaStream_t)stream);
+}
+
+}  // extern "C"

@@ -1,0 +1,126 @@
+// Shared helpers for the regridding_gb300 CUDA library (sm_103a).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+#include <string>
+
+#include "../../include/regrid_gb300.h"
+
+namespace rg {
+
+// ---------------------------------------------------------------------------
+// error reporting: every C entry point returns an RG_* status and records a
+// message retrievable through rg_last_error (thread-local).
+// ---------------------------------------------------------------------------
+void set_error(const char* fmt, ...);
+const char* last_error();
+
+#define RG_CUDA(call)                                                                  \
+    do {                                                                               \
+        cudaError_t _e = (call);                                                       \
+        if (_e != cudaSuccess) {                                                       \
+            ::rg::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call,                 \
+                            cudaGetErrorString(_e));                                   \
+            return RG_ERR_CUDA;                                                        \
+        }                                                                              \
+    } while (0)
+
+#define RG_CHECK(cond, status, ...)                                                    \
+    do {                                                                               \
+        if (!(cond)) {                                                                 \
+            ::rg::set_error(__VA_ARGS__);                                              \
+            return (status);                                                           \
+        }                                                                              \
+    } while (0)
+
+#define RG_TRY(expr)                                                                   \
+    do {                                                                               \
+        int _s = (expr);                                                               \
+        if (_s != RG_OK) return _s;                                                    \
+    } while (0)
+
+// Device-side error flag bits, written with atomicOr by kernels that detect a
+// condition they cannot handle (a walk exceeding its step cap, a seat outside
+// the grid, an over-long bucket).  The host reads the word after the launch
+// sequence and turns it into a status.
+enum DeviceFlag : unsigned {
+    FLAG_WALK_CAP = 1u << 0,
+    FLAG_SEAT_OUTSIDE = 1u << 1,
+    FLAG_BUCKET_TOO_LONG = 1u << 2,
+    FLAG_CAPACITY = 1u << 3,
+};
+
+// ---------------------------------------------------------------------------
+// IEEE double arithmetic with one rounding per operation.  The upstream
+// algorithms are defined by their (unfused) Python arithmetic, so every FP64
+// expression whose result decides a branch or is emitted as a weight is spelt
+// with these intrinsics, which the compiler never contracts into an FMA.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dadd(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double dsub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dmul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a, b); }
+
+constexpr int64_t MAXSIZE = INT64_MAX;  // sys.maxsize: the upstream out-of-grid sentinel
+
+// simple RAII-free device buffer helpers (stream ordered)
+template <typename T>
+int dalloc(T** p, size_t n, cudaStream_t s) {
+    *p = nullptr;
+    if (n == 0) n = 1;
+    cudaError_t e = cudaMallocAsync((void**)p, n * sizeof(T), s);
+    if (e != cudaSuccess) {
+        set_error("cudaMallocAsync(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
+        return RG_ERR_ALLOC;
+    }
+    return RG_OK;
+}
+template <typename T>
+void dfree(T* p, cudaStream_t s) {
+    if (p) cudaFreeAsync((void*)p, s);
+}
+
+inline unsigned grid_for(int64_t n, int block) {
+    int64_t g = (n + block - 1) / block;
+    if (g < 1) g = 1;
+    if (g > 0x7fffffff) g = 0x7fffffff;
+    return (unsigned)g;
+}
+
+// device-wide exclusive scan of n int64 values (in may equal out); writes the
+// total to *total_dev if non-null.  Implemented in scan.cu.
+int exclusive_scan_i64(const int64_t* in, int64_t* out, int64_t n, int64_t* total_dev,
+                       cudaStream_t s);
+int exclusive_scan_u32_to_i64(const unsigned* in, int64_t* out, int64_t n, int64_t* total_dev,
+                              cudaStream_t s);
+
+// Stable ordering of elements grouped into buckets: given bucket[k] in
+// [0, nbuckets) and a secondary key skey[k] that is unique within each bucket,
+// produce bucket_ptr[nbuckets+1] and perm[n] such that perm lists the
+// elements sorted by (bucket, skey).  Implemented in sort.cu.
+int bucket_sort(const int32_t* bucket, const int64_t* skey, int64_t n, int64_t nbuckets,
+                int64_t* bucket_ptr, uint32_t* perm, unsigned* flags, cudaStream_t s);
+
+}  // namespace rg
+
+// Opaque weight matrix of one orthogonal element, resident on the device.
+// Rows are output cells, columns input cells; entries of each row are sorted
+// by column, which is also the order the upstream apply accumulates them.
+struct rg_weights_s {
+    int64_t n_in = 0, n_out = 0, nnz = 0;
+    int64_t* row_ptr = nullptr;  // [n_out + 1]
+    int32_t* col = nullptr;      // [nnz]
+    double* val = nullptr;       // [nnz]
+    float* val32 = nullptr;      // lazily made float32 copy of val
+    // transposed (rows = input cells), built on demand for the transposed apply
+    int64_t* t_row_ptr = nullptr;
+    int32_t* t_col = nullptr;
+    double* t_val = nullptr;
+    float* t_val32 = nullptr;
+    // (optional) output grid shape for 2D tiling of the apply
+    int64_t out_shape0 = 0, out_shape1 = 0;
+    int device = 0;
+};

@@ -1,0 +1,1026 @@
+// Conservative 2D weights on the GPU: the Ramshaw (1985) edge sweep.
+//
+// Every grid line of the output grid is traced through the cells of the input
+// grid and every grid line of the input grid through the cells of the output
+// grid.  Each piece of a line inside one cell of the other grid contributes
+// the contour integral 1/2 (x1 y2 - x2 y1) to the two cells of its own grid
+// that it separates (Green's theorem); the contributions of one
+// (input, output) pair sum to their overlap area.
+//
+// The walk follows regridding/_weights/_weights_conservative_2d/
+// _weights_conservative_2d.py:206-912 step for step with the same IEEE double
+// arithmetic (one rounding per operation, no FMA), so crossing decisions,
+// emitted triples and their order are identical to the upstream code.  What
+// is GB300-specific is the organisation:
+//   * seat kernel: one warp per sweep line computes the line's starting state
+//     (the O(perimeter) winding-number test is split across the lanes; its
+//     partial sums are multiples of 1/2 and therefore exact in any order);
+//   * walk kernel: one thread per sweep line, run twice (count, then write at
+//     scanned offsets), which reproduces the upstream emission order without
+//     a sort on sequence numbers;
+//   * the O(perimeter) search for re-entry into the static grid
+//     (_step_outside_static, :547-698) is answered from a uniform bin grid of
+//     the static boundary, evaluating exactly the candidate edges whose
+//     bounding boxes can pass the upstream box test and keeping the upstream
+//     "first smallest t" choice;
+//   * merge: raw triples are bucketed by output cell, ranked by (input,
+//     emission position) inside each bucket, and equal pairs are summed with
+//     numpy's add.reduceat association (first + pairwise rest), giving a CSR
+//     matrix whose values are bit-identical to the upstream coalesced ones.
+#include <cmath>
+
+#include "common.cuh"
+
+namespace rg {
+namespace {
+
+// ---------------------------------------------------------------------------
+// geometry (regridding/geometry.py)
+// ---------------------------------------------------------------------------
+
+// bounding_boxes_intersect_2d: geometry.py:153-284
+__device__ __forceinline__ bool bboxes_intersect(double xp1, double yp1, double xp2, double yp2,
+                                                 double xq1, double yq1, double xq2, double yq2) {
+    double t;
+    if (xp1 > xp2) { t = xp1; xp1 = xp2; xp2 = t; }
+    if (xq1 > xq2) { t = xq1; xq1 = xq2; xq2 = t; }
+    if (!(xp1 <= xq2 && xq1 <= xp2)) return false;
+    if (yp1 > yp2) { t = yp1; yp1 = yp2; yp2 = t; }
+    if (yq1 > yq2) { t = yq1; yq1 = yq2; yq2 = t; }
+    if (!(yp1 <= yq2 && yq1 <= yp2)) return false;
+    return true;
+}
+
+// two_line_segment_intersection_parameters (geometry.py:370-445) followed by
+// two_line_segments_intersect (geometry.py:448-475, half-open 0 <= t,u < 1).
+__device__ __forceinline__ bool seg_hit(double x1, double y1, double x2, double y2, double x3,
+                                        double y3, double x4, double y4, double* t_out) {
+    if (!bboxes_intersect(x1, y1, x2, y2, x3, y3, x4, y4)) return false;
+    double tdet = dsub(dmul(dsub(x1, x3), dsub(y3, y4)), dmul(dsub(y1, y3), dsub(x3, x4)));
+    double udet = dsub(dmul(dsub(x1, x2), dsub(y1, y3)), dmul(dsub(y1, y2), dsub(x1, x3)));
+    double det = dsub(dmul(dsub(x1, x2), dsub(y3, y4)), dmul(dsub(y1, y2), dsub(x3, x4)));
+    double t = ddiv(tdet, det);
+    double u = ddiv(-udet, det);
+    *t_out = t;
+    return (0 <= t && t < 1) && (0 <= u && u < 1);
+}
+
+// contribution of one boundary edge to the extended winding number of
+// point_is_inside_polygon (geometry.py:737-829)
+__device__ __forceinline__ double winding_term(double x, double y, double vx0, double vy0,
+                                               double vx1, double vy1) {
+    double x0 = dsub(vx0, x), y0 = dsub(vy0, y);
+    double x1 = dsub(vx1, x), y1 = dsub(vy1, y);
+    if (dmul(y0, y1) < 0) {
+        double r = dadd(x0, ddiv(dmul(y0, dsub(x1, x0)), dsub(y0, y1)));
+        if (r > 0) return (y0 < 0) ? 1.0 : -1.0;
+        return (y0 < 0) ? -1.0 : 1.0;
+    } else if (y0 == 0) {
+        if (x0 > 0) {
+            if (y1 > 0) return 0.5;
+            if (y1 < 0) return -0.5;
+        } else if (x0 < 0) {
+            if (y1 < 0) return 0.5;
+            if (y1 > 0) return -0.5;
+        }
+    } else if (y1 == 0) {
+        if (x1 > 0) {
+            if (y0 < 0) return 0.5;
+            if (y0 > 0) return -0.5;
+        } else if (x1 < 0) {
+            if (y0 > 0) return 0.5;
+            if (y0 < 0) return -0.5;
+        }
+    }
+    return 0.0;
+}
+
+struct Grid {
+    const double* x;
+    const double* y;
+    int64_t nx, ny;
+    __device__ __forceinline__ double X(int64_t i, int64_t j) const { return __ldg(x + i * ny + j); }
+    __device__ __forceinline__ double Y(int64_t i, int64_t j) const { return __ldg(y + i * ny + j); }
+};
+
+// point_is_inside_polygon on the 4 vertices of cell (i, j) in the order
+// (i,j), (i+1,j), (i+1,j+1), (i,j+1) (_grids.py:251-276)
+__device__ bool cell_contains(const Grid& g, int64_t i, int64_t j, double px, double py) {
+    double vx[4], vy[4];
+    vx[0] = g.X(i, j);         vy[0] = g.Y(i, j);
+    vx[1] = g.X(i + 1, j);     vy[1] = g.Y(i + 1, j);
+    vx[2] = g.X(i + 1, j + 1); vy[2] = g.Y(i + 1, j + 1);
+    vx[3] = g.X(i, j + 1);     vy[3] = g.Y(i, j + 1);
+    double w = 0;
+#pragma unroll
+    for (int v = 0; v < 4; v++) {
+        int p = (v + 3) & 3;
+        w = w + winding_term(px, py, vx[p], vy[p], vx[v], vy[v]);
+    }
+    return w != 0;
+}
+
+// _index_of_point_local: _grids.py:282-349
+__device__ void locate_local(const Grid& g, double px, double py, int64_t i0, int64_t j0,
+                             int64_t* oi, int64_t* oj) {
+    int64_t ncx = g.nx - 1, ncy = g.ny - 1;
+    int64_t ia = i0 - 1 > 0 ? i0 - 1 : 0, ib = i0 + 2 < ncx ? i0 + 2 : ncx;
+    int64_t ja = j0 - 1 > 0 ? j0 - 1 : 0, jb = j0 + 2 < ncy ? j0 + 2 : ncy;
+    for (int64_t ii = ia; ii < ib; ii++)
+        for (int64_t jj = ja; jj < jb; jj++)
+            if (cell_contains(g, ii, jj, px, py)) {
+                *oi = ii;
+                *oj = jj;
+                return;
+            }
+    *oi = MAXSIZE;
+    *oj = MAXSIZE;
+}
+
+// _bilinear_interpolation: regridding/_interp_ndarray.py:226-269
+__device__ double bilinear(const double* a, int64_t sx, int64_t sy, double x, double y) {
+    int64_t x00 = (int64_t)floor(x), y00 = (int64_t)floor(y);
+    if (x00 < 0) x00 = 0;
+    else if (x00 > sx - 2) x00 = sx - 2;
+    if (y00 < 0) y00 = 0;
+    else if (y00 > sy - 2) y00 = sy - 2;
+    double a00 = __ldg(a + x00 * sy + y00), a01 = __ldg(a + x00 * sy + y00 + 1);
+    double a10 = __ldg(a + (x00 + 1) * sy + y00), a11 = __ldg(a + (x00 + 1) * sy + y00 + 1);
+    double dx = dsub(x, (double)x00), dy = dsub(y, (double)y00);
+    double w00 = dmul(dsub(1.0, dx), dsub(1.0, dy)), w01 = dmul(dsub(1.0, dx), dy);
+    double w10 = dmul(dx, dsub(1.0, dy)), w11 = dmul(dx, dy);
+    return dadd(dadd(dadd(dmul(a00, w00), dmul(a01, w01)), dmul(a10, w10)), dmul(a11, w11));
+}
+
+__device__ __forceinline__ bool floor_ok(double v) { return isfinite(v) && fabs(v) < 9.0e18; }
+
+// index_of_point_secant: _grids.py:352-463.  Returns false when the upstream
+// falls back to index_of_point_brute (singular Jacobian, no convergence, or an
+// iterate the upstream could not floor).
+__device__ bool locate_secant(const Grid& g, double px, double py, int64_t* oi, int64_t* oj) {
+    const double h = 1e-3;
+    int64_t sx = g.nx, sy = g.ny;
+    double i = (double)sx / 2, j = (double)sy / 2;
+    for (int it = 0; it < 100; it++) {
+        double xv = bilinear(g.x, sx, sy, i, j);
+        double yv = bilinear(g.y, sx, sy, i, j);
+        if (!floor_ok(i) || !floor_ok(j)) return false;
+        int64_t i0 = (int64_t)floor(i), j0 = (int64_t)floor(j);
+        double ex = dsub(xv, px), ey = dsub(yv, py);
+        if (i0 >= 0 && j0 >= 0 && i0 < sx - 1 && j0 < sy - 1) {
+            if (cell_contains(g, i0, j0, px, py)) {
+                locate_local(g, px, py, i0, j0, oi, oj);
+                return true;
+            }
+        }
+        if (fabs(ex) < 1e-10 && fabs(ey) < 1e-10) {
+            locate_local(g, px, py, i0, j0, oi, oj);
+            return true;
+        }
+        double dx_di = ddiv(dsub(bilinear(g.x, sx, sy, dadd(i, h), j), xv), h);
+        double dx_dj = ddiv(dsub(bilinear(g.x, sx, sy, i, dadd(j, h)), xv), h);
+        double dy_di = ddiv(dsub(bilinear(g.y, sx, sy, dadd(i, h), j), yv), h);
+        double dy_dj = ddiv(dsub(bilinear(g.y, sx, sy, i, dadd(j, h)), yv), h);
+        double det = dsub(dmul(dx_di, dy_dj), dmul(dx_dj, dy_di));
+        if (det == 0) return false;
+        double di = ddiv(dsub(dmul(dy_dj, ex), dmul(dx_dj, ey)), det);
+        double dj = ddiv(dadd(dmul(-dy_di, ex), dmul(dx_di, ey)), det);
+        i = dsub(i, di);
+        j = dsub(j, dj);
+    }
+    return false;
+}
+
+// index_of_point_brute (_grids.py:218-279) by one warp: lanes test 32
+// consecutive cells of the upstream (i outer, j inner) order per round and
+// the first containing cell of the first round with a hit wins.
+__device__ void locate_brute_warp(const Grid& g, double px, double py, int64_t* oi, int64_t* oj) {
+    int lane = threadIdx.x & 31;
+    int64_t ncx = g.nx - 1, ncy = g.ny - 1, ncells = ncx * ncy;
+    for (int64_t base = 0; base < ncells; base += 32) {
+        int64_t k = base + lane;
+        bool hit = k < ncells && cell_contains(g, k / ncy, k % ncy, px, py);
+        unsigned m = __ballot_sync(0xffffffffu, hit);
+        if (m) {
+            int64_t kk = base + __ffs(m) - 1;
+            *oi = kk / ncy;
+            *oj = kk % ncy;
+            return;
+        }
+    }
+    *oi = MAXSIZE;
+    *oj = MAXSIZE;
+}
+
+// ---------------------------------------------------------------------------
+// per-grid preparation
+// ---------------------------------------------------------------------------
+
+// grid_volume: _grids.py:50-140.  One thread per cell; the four contour terms
+// are added in the upstream order (((0 - A) + B) - C) + D.
+__global__ void cell_area_kernel(const double* __restrict__ x, const double* __restrict__ y,
+                                 int64_t nx, int64_t ny, double* __restrict__ out) {
+    int64_t ncx = nx - 1, ncy = ny - 1;
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncx * ncy;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int64_t p = c / ncy, q = c % ncy;
+        double x00 = x[p * ny + q], y00 = y[p * ny + q];
+        double x10 = x[(p + 1) * ny + q], y10 = y[(p + 1) * ny + q];
+        double x01 = x[p * ny + q + 1], y01 = y[p * ny + q + 1];
+        double x11 = x[(p + 1) * ny + q + 1], y11 = y[(p + 1) * ny + q + 1];
+        // axis 0 (transposed, coordinates swapped)
+        double A = dmul(dsub(dmul(y00, x10), dmul(y10, x00)), 0.5);
+        double B = dmul(dsub(dmul(y01, x11), dmul(y11, x01)), 0.5);
+        // axis 1
+        double C = dmul(dsub(dmul(x00, y01), dmul(x01, y00)), 0.5);
+        double D = dmul(dsub(dmul(x10, y11), dmul(x11, y10)), 0.5);
+        double v = dsub(0.0, A);
+        v = dadd(v, B);
+        v = dsub(v, C);
+        v = dadd(v, D);
+        out[c] = v;
+    }
+}
+
+__global__ void bbox_kernel(const double* x, const double* y, int64_t n, double* out4) {
+    // out4 = (xmin, ymin, xmax, ymax); single block
+    __shared__ double s[4][256];
+    double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+        double xv = x[k], yv = y[k];
+        a = fmin(a, xv);
+        b = fmin(b, yv);
+        c = fmax(c, xv);
+        d = fmax(d, yv);
+    }
+    s[0][threadIdx.x] = a;
+    s[1][threadIdx.x] = b;
+    s[2][threadIdx.x] = c;
+    s[3][threadIdx.x] = d;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            s[0][threadIdx.x] = fmin(s[0][threadIdx.x], s[0][threadIdx.x + w]);
+            s[1][threadIdx.x] = fmin(s[1][threadIdx.x], s[1][threadIdx.x + w]);
+            s[2][threadIdx.x] = fmax(s[2][threadIdx.x], s[2][threadIdx.x + w]);
+            s[3][threadIdx.x] = fmax(s[3][threadIdx.x], s[3][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) out4[threadIdx.x] = s[threadIdx.x][0];
+}
+
+// Boundary polygon of grid_boundary (_grids.py:167-215), vertex k.
+__device__ __forceinline__ void boundary_vertex(const Grid& g, int64_t k, double* bx, double* by) {
+    int64_t sx = g.nx, sy = g.ny;
+    int64_t i, j;
+    if (k < sx - 1) { i = k; j = 0; }
+    else if ((k -= sx - 1) < sy - 1) { i = sx - 1; j = k; }
+    else if ((k -= sy - 1) < sx - 1) { i = sx - 1 - k; j = sy - 1; }
+    else { k -= sx - 1; i = 0; j = sy - 1 - k; }
+    *bx = g.X(i, j);
+    *by = g.Y(i, j);
+}
+
+// Boundary edges in the scan order of _step_outside_static (:608-683):
+// axis 0 (faces i = 0 then i = nx-1, running along j), then axis 1 (faces
+// j = 0 then j = ny-1, running along i).
+struct Edge {
+    double x3, y3, x4, y4;
+    int64_t cell;  // flat static cell index
+    int code;      // direction_face * 2 + axis = the cell edge it enters through
+    int pad;
+};
+
+__global__ void boundary_edges_kernel(Grid g, Edge* edges, int64_t nedges) {
+    int64_t ncx = g.nx - 1, ncy = g.ny - 1;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nedges;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        int axis, dir;
+        int64_t i0, kk = k;
+        if (kk < 2 * ncy) {
+            axis = 0;
+            dir = kk >= ncy;
+            i0 = kk - dir * ncy;
+        } else {
+            kk -= 2 * ncy;
+            axis = 1;
+            dir = kk >= ncx;
+            i0 = kk - dir * ncx;
+        }
+        Edge e;
+        if (axis == 0) {
+            int64_t ie = dir ? g.nx - 1 : 0;
+            e.x3 = g.X(ie, i0); e.y3 = g.Y(ie, i0);
+            e.x4 = g.X(ie, i0 + 1); e.y4 = g.Y(ie, i0 + 1);
+            int64_t cx = dir ? ncx - 1 : 0;
+            e.cell = cx * ncy + i0;
+        } else {
+            int64_t je = dir ? g.ny - 1 : 0;
+            e.x3 = g.X(i0, je); e.y3 = g.Y(i0, je);
+            e.x4 = g.X(i0 + 1, je); e.y4 = g.Y(i0 + 1, je);
+            int64_t cy = dir ? ncy - 1 : 0;
+            e.cell = i0 * ncy + cy;
+        }
+        e.code = dir * 2 + axis;
+        e.pad = 0;
+        edges[k] = e;
+    }
+}
+
+struct Bins {
+    double ox, oy, inv_h;
+    int nbx, nby;
+    const int32_t* ptr;    // [nbx*nby + 1]
+    const int32_t* items;  // edge indices
+};
+
+__device__ __forceinline__ int bin_coord(double v, double o, double inv_h, int nb) {
+    double f = floor(dmul(dsub(v, o), inv_h));
+    if (!(f >= 0)) return 0;  // also maps NaN to 0
+    if (f >= nb - 1) return nb - 1;
+    return (int)f;
+}
+
+template <bool FILL>
+__global__ void bin_edges_kernel(const Edge* edges, int64_t nedges, Bins b, unsigned* counts,
+                                 int32_t* items, const int64_t* ptr64) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nedges;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        Edge e = edges[k];
+        int bx0 = bin_coord(fmin(e.x3, e.x4), b.ox, b.inv_h, b.nbx);
+        int bx1 = bin_coord(fmax(e.x3, e.x4), b.ox, b.inv_h, b.nbx);
+        int by0 = bin_coord(fmin(e.y3, e.y4), b.oy, b.inv_h, b.nby);
+        int by1 = bin_coord(fmax(e.y3, e.y4), b.oy, b.inv_h, b.nby);
+        for (int by = by0; by <= by1; by++)
+            for (int bx = bx0; bx <= bx1; bx++) {
+                int64_t bin = (int64_t)by * b.nbx + bx;
+                unsigned pos = atomicAdd(&counts[bin], 1u);
+                if (FILL) items[ptr64[bin] + pos] = (int32_t)k;
+            }
+    }
+}
+
+__global__ void i64_to_i32(const int64_t* a, int32_t* b, int64_t n) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        b[k] = (int32_t)a[k];
+}
+
+// ---------------------------------------------------------------------------
+// sweep families and line seats
+// ---------------------------------------------------------------------------
+
+struct Static {
+    Grid g;
+    int64_t ncx, ncy;
+    double blx, bly, bux, buy;
+    int64_t nbound;  // boundary polygon vertices
+    const Edge* edges;
+    Bins bins;
+};
+
+struct Family {
+    Grid sweep;        // unaligned sweep grid
+    int transposed;    // axis_sweep == 0
+    int64_t lines;     // aligned rows
+    int64_t len;       // aligned columns (vertices along a line)
+    int sweep_input;
+    int axis;
+    int st;            // 0: static = input grid, 1: static = output grid
+    int64_t line_base;
+    __device__ __forceinline__ double SX(int64_t a, int64_t b) const {
+        return transposed ? sweep.X(b, a) : sweep.X(a, b);
+    }
+    __device__ __forceinline__ double SY(int64_t a, int64_t b) const {
+        return transposed ? sweep.Y(b, a) : sweep.Y(a, b);
+    }
+};
+
+struct SweepParams {
+    Family fam[4];
+    Static st[2];
+    const double* area_in;  // (ncx_in, ncy_in)
+    const double* w_in;     // nullable
+    int64_t ncy_in, ncy_out;
+    int64_t total_lines;
+};
+
+struct Seat {
+    int64_t stx, sty;
+    int outside;
+    int pad;
+};
+
+__device__ __forceinline__ int family_of(const SweepParams& P, int64_t line) {
+    int f = 0;
+#pragma unroll
+    for (int k = 1; k < 4; k++)
+        if (line >= P.fam[k].line_base) f = k;
+    return f;
+}
+
+// Starting state of every sweep line (:439-468): one warp per line.
+__global__ void __launch_bounds__(128) seat_kernel(SweepParams P, Seat* seats, unsigned* flags) {
+    int lane = threadIdx.x & 31;
+    int64_t line = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (line >= P.total_lines) return;
+    const Family& F = P.fam[family_of(P, line)];
+    const Static& S = P.st[F.st];
+    int64_t li = line - F.line_base;
+    double x1 = F.SX(li, 0), y1 = F.SY(li, 0);
+    Seat seat;
+    seat.stx = MAXSIZE;
+    seat.sty = MAXSIZE;
+    seat.outside = 1;
+    seat.pad = 0;
+    bool in_box = (S.blx <= x1 && x1 <= S.bux) && (S.bly <= y1 && y1 <= S.buy);
+    if (in_box) {
+        double w = 0;
+        for (int64_t v = lane; v < S.nbound; v += 32) {
+            double ax, ay, bx, by;
+            boundary_vertex(S.g, v == 0 ? S.nbound - 1 : v - 1, &ax, &ay);
+            boundary_vertex(S.g, v, &bx, &by);
+            w += winding_term(x1, y1, ax, ay, bx, by);
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);
+        if (w != 0) {
+            int64_t i = MAXSIZE, j = MAXSIZE;
+            int ok = 0;
+            if (lane == 0) ok = locate_secant(S.g, x1, y1, &i, &j);
+            ok = __shfl_sync(0xffffffffu, ok, 0);
+            if (!ok) locate_brute_warp(S.g, x1, y1, &i, &j);
+            seat.stx = i;
+            seat.sty = j;
+            seat.outside = 0;
+            if (i == MAXSIZE) atomicOr(flags, FLAG_SEAT_OUTSIDE);
+        }
+    }
+    if (lane == 0) seats[line] = seat;
+}
+
+// ---------------------------------------------------------------------------
+// the walk
+// ---------------------------------------------------------------------------
+
+__constant__ int c_vtx_i[4] = {0, 1, 1, 0};   // indices_cell_vertex: _grids.py:153-158
+__constant__ int c_vtx_j[4] = {0, 0, 1, 1};
+__constant__ int c_nrm_i[4] = {-1, 0, 1, 0};  // cell_normals: _grids.py:143-148
+__constant__ int c_nrm_j[4] = {0, -1, 0, 1};
+
+// One thread per sweep line: the body of the prange loop of _sweep_along_axis
+// (:432-533) with _step_outside_static (:547-698), _step_inside_static
+// (:707-895) and _calc_and_save_weights (:903-976) inlined.  COUNT mode only
+// counts the triples a line emits; WRITE mode stores them from offsets[line].
+template <bool WRITE>
+__global__ void __launch_bounds__(64)
+    walk_kernel(SweepParams P, const Seat* __restrict__ seats, int64_t* __restrict__ counts,
+                const int64_t* __restrict__ offsets, int32_t* __restrict__ raw_in,
+                int32_t* __restrict__ raw_out, double* __restrict__ raw_val, unsigned* flags) {
+    int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (line >= P.total_lines) return;
+    const Family F = P.fam[family_of(P, line)];
+    const Static& S = P.st[F.st];
+    const Grid st = S.g;
+    const int64_t li = line - F.line_base;
+    Seat seat = seats[line];
+    int64_t stx = seat.stx, sty = seat.sty;
+    bool outside = seat.outside;
+    int64_t edge_last = MAXSIZE;
+    int64_t sy_idx = 0;
+    int64_t n_emit = 0;
+    int64_t wpos = WRITE ? offsets[line] : 0;
+    const int64_t max_steps = 64 * (F.len + 4 * (S.ncx + S.ncy) + 16);
+    int64_t steps = 0;
+    double x1 = F.SX(li, 0), y1 = F.SY(li, 0);
+
+    while (sy_idx < F.len - 1) {
+        if (++steps > max_steps) {
+            atomicOr(flags, FLAG_WALK_CAP);
+            break;
+        }
+        double x2 = F.SX(li, sy_idx + 1), y2 = F.SY(li, sy_idx + 1);
+        if (outside) {
+            // _step_outside_static: smallest-t crossing of the static boundary,
+            // candidates from the bins overlapping the segment's box
+            const double p2x = x2, p2y = y2;
+            double sminx = fmin(x1, p2x), smaxx = fmax(x1, p2x);
+            double sminy = fmin(y1, p2y), smaxy = fmax(y1, p2y);
+            bool found = false;
+            double t_min = INFINITY;
+            int64_t best_order = INT64_MAX;
+            int best_code = 0;
+            int64_t best_cell = 0;
+            if (!(smaxx < S.blx || sminx > S.bux || smaxy < S.bly || sminy > S.buy)) {
+                const Bins& B = S.bins;
+                int bx0 = bin_coord(sminx, B.ox, B.inv_h, B.nbx);
+                int bx1 = bin_coord(smaxx, B.ox, B.inv_h, B.nbx);
+                int by0 = bin_coord(sminy, B.oy, B.inv_h, B.nby);
+                int by1 = bin_coord(smaxy, B.oy, B.inv_h, B.nby);
+                for (int by = by0; by <= by1; by++) {
+                    for (int bx = bx0; bx <= bx1; bx++) {
+                        int64_t bin = (int64_t)by * B.nbx + bx;
+                        int32_t s0 = __ldg(B.ptr + bin), s1 = __ldg(B.ptr + bin + 1);
+                        for (int32_t q = s0; q < s1; q++) {
+                            int32_t ek = __ldg(B.items + q);
+                            const Edge e = S.edges[ek];
+                            double t;
+                            if (!seg_hit(x1, y1, p2x, p2y, e.x3, e.y3, e.x4, e.y4, &t)) continue;
+                            if (e.cell == edge_last) continue;
+                            if (t < t_min || (t == t_min && ek < best_order)) {
+                                t_min = t;
+                                best_order = ek;
+                                best_code = e.code;
+                                best_cell = e.cell;
+                                found = true;
+                            }
+                        }
+                    }
+                }
+            }
+            if (found) {
+                stx = best_cell / S.ncy;
+                sty = best_cell % S.ncy;
+                x2 = dadd(x1, dmul(t_min, dsub(p2x, x1)));
+                y2 = dadd(y1, dmul(t_min, dsub(p2y, y1)));
+                edge_last = best_code;
+                outside = false;
+            } else {
+                edge_last = MAXSIZE;
+                sy_idx = sy_idx + 1;
+            }
+        } else {
+            // _step_inside_static: first crossed edge of the current static
+            // cell other than the entry edge
+            const double p2x = x2, p2y = y2;
+            int found = -1;
+#pragma unroll 1
+            for (int v = 0; v < 4; v++) {
+                if (v == edge_last) continue;
+                int vp = (v + 3) & 3;
+                double x3 = st.X(stx + c_vtx_i[vp], sty + c_vtx_j[vp]);
+                double y3 = st.Y(stx + c_vtx_i[vp], sty + c_vtx_j[vp]);
+                double x4 = st.X(stx + c_vtx_i[v], sty + c_vtx_j[v]);
+                double y4 = st.Y(stx + c_vtx_i[v], sty + c_vtx_j[v]);
+                double t;
+                if (seg_hit(x1, y1, p2x, p2y, x3, y3, x4, y4, &t)) {
+                    x2 = dadd(x1, dmul(t, dsub(p2x, x1)));
+                    y2 = dadd(y1, dmul(t, dsub(p2y, y1)));
+                    found = v;
+                    break;
+                }
+            }
+            int64_t nsy, nstx, nsty;
+            if (found >= 0) {
+                nsy = sy_idx;
+                nstx = stx + c_nrm_i[found];
+                nsty = sty + c_nrm_j[found];
+                edge_last = (found + 2) % 4;
+            } else {
+                nsy = sy_idx + 1;
+                nstx = stx;
+                nsty = sty;
+                edge_last = MAXSIZE;
+            }
+            // _calc_and_save_weights: area_triangle, negated for axis 0
+            double area = dmul(dsub(dmul(x1, y2), dmul(x2, y1)), 0.5);
+            if (F.axis == 0) area = -area;
+#pragma unroll
+            for (int side = 0; side < 2; side++) {
+                int64_t is = side == 0 ? li - 1 : li;
+                if (side == 0 && !(is >= 0)) continue;
+                if (side == 1 && !(is < F.lines - 1)) continue;
+                int64_t a = is, b = sy_idx;
+                if (F.axis == 0) { a = sy_idx; b = is; }
+                int64_t ii, ij, oi, oj;
+                if (F.sweep_input) { ii = a; ij = b; oi = stx; oj = sty; }
+                else { ii = stx; ij = sty; oi = a; oj = b; }
+                int64_t in_flat = ii * P.ncy_in + ij;
+                if (WRITE) {
+                    double ain = __ldg(P.area_in + in_flat);
+                    double w = side == 0 ? ddiv(area, ain) : ddiv(-area, ain);
+                    if (P.w_in) w = dmul(w, __ldg(P.w_in + in_flat));
+                    raw_in[wpos] = (int32_t)in_flat;
+                    raw_out[wpos] = (int32_t)(oi * P.ncy_out + oj);
+                    raw_val[wpos] = w;
+                    wpos++;
+                }
+                n_emit++;
+            }
+            if (!(nstx >= 0 && nsty >= 0 && nstx < S.ncx && nsty < S.ncy)) {
+                edge_last = stx * S.ncy + sty;
+                nstx = MAXSIZE;
+                nsty = MAXSIZE;
+                outside = true;
+            }
+            sy_idx = nsy;
+            stx = nstx;
+            sty = nsty;
+        }
+        x1 = x2;
+        y1 = y2;
+    }
+    if (!WRITE) counts[line] = n_emit;
+}
+
+// ---------------------------------------------------------------------------
+// merge (regridding/_weights/_weights_arrays.py:44-73)
+// ---------------------------------------------------------------------------
+
+__global__ void make_keys(const int32_t* raw_in, int64_t n, int64_t* skey) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x)
+        skey[k] = ((int64_t)raw_in[k] << 32) | (int64_t)(uint32_t)k;
+}
+
+// numpy's pairwise summation for n <= 128 (used by add.reduce / reduceat):
+// a sequential sum from -0.0 below 8 terms, else 8 interleaved partial sums.
+template <typename At>
+__device__ double pw_block(const At& at, int64_t off, int64_t n) {
+    if (n < 8) {
+        double res = -0.0;
+        for (int64_t i = 0; i < n; i++) res = dadd(res, at(off + i));
+        return res;
+    }
+    double r[8];
+#pragma unroll
+    for (int j = 0; j < 8; j++) r[j] = at(off + j);
+    int64_t i = 8;
+    for (; i < n - (n % 8); i += 8) {
+#pragma unroll
+        for (int j = 0; j < 8; j++) r[j] = dadd(r[j], at(off + i + j));
+    }
+    double res = dadd(dadd(dadd(r[0], r[1]), dadd(r[2], r[3])), dadd(dadd(r[4], r[5]), dadd(r[6], r[7])));
+    for (; i < n; i++) res = dadd(res, at(off + i));
+    return res;
+}
+
+// numpy pairwise_sum: blocks of at most 128 terms, larger ranges split at
+// n/2 rounded down to a multiple of 8 (iterative form of the recursion)
+template <typename At>
+__device__ double pairwise_sum(const At& at, int64_t off, int64_t n) {
+    struct Frame {
+        int64_t off, n;
+        double left;
+        int stage;
+    };
+    Frame stk[48];
+    int sp = 0;
+    stk[0] = {off, n, 0.0, 0};
+    for (;;) {
+        Frame& f = stk[sp];
+        if (f.n <= 128) {
+            double result = pw_block(at, f.off, f.n);
+            for (;;) {
+                if (sp == 0) return result;
+                sp--;
+                Frame& p = stk[sp];
+                if (p.stage == 1) {
+                    p.left = result;
+                    p.stage = 2;
+                    int64_t n2 = p.n / 2;
+                    n2 -= n2 % 8;
+                    stk[sp + 1] = {p.off + n2, p.n - n2, 0.0, 0};
+                    sp++;
+                    break;
+                }
+                result = dadd(p.left, result);
+            }
+        } else {
+            f.stage = 1;
+            int64_t n2 = f.n / 2;
+            n2 -= n2 % 8;
+            stk[sp + 1] = {f.off, n2, 0.0, 0};
+            sp++;
+        }
+    }
+}
+
+struct GatherVal {
+    const double* val;
+    const uint32_t* perm;
+    __device__ __forceinline__ double operator()(int64_t k) const { return val[perm[k]]; }
+};
+
+// One thread per output cell: merge equal input indices of the cell's sorted
+// raw entries with the add.reduceat association, first + pairwise(rest),
+// writing (col, value) compactly from the bucket start; count them.
+__global__ void merge_rows(const int64_t* __restrict__ bptr, const uint32_t* __restrict__ perm,
+                           const int32_t* __restrict__ raw_in, const double* __restrict__ raw_val,
+                           int64_t n_out, int32_t* __restrict__ tmp_col, double* __restrict__ tmp_val,
+                           int64_t* __restrict__ row_nnz) {
+    GatherVal at{raw_val, perm};
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = bptr[o], t = bptr[o + 1];
+        int64_t w = s;
+        int64_t g = s;
+        while (g < t) {
+            int32_t c = raw_in[perm[g]];
+            int64_t h = g + 1;
+            while (h < t && raw_in[perm[h]] == c) h++;
+            double v = dadd(at(g), pairwise_sum(at, g + 1, h - g - 1));
+            tmp_col[w] = c;
+            tmp_val[w] = v;
+            w++;
+            g = h;
+        }
+        row_nnz[o] = w - s;
+    }
+}
+
+__global__ void compact_rows(const int64_t* __restrict__ bptr, const int64_t* __restrict__ row_ptr,
+                             const int32_t* __restrict__ tmp_col, const double* __restrict__ tmp_val,
+                             int64_t n_out, int32_t* __restrict__ col, double* __restrict__ val) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out;
+         o += (int64_t)gridDim.x * blockDim.x) {
+        int64_t s = bptr[o], d = row_ptr[o], n = row_ptr[o + 1] - d;
+        for (int64_t k = 0; k < n; k++) {
+            col[d + k] = tmp_col[s + k];
+            val[d + k] = tmp_val[s + k];
+        }
+    }
+}
+
+int prepare_static(const double* x, const double* y, int64_t nx, int64_t ny, const double* bbox_h,
+                   Static* S, Edge** edges_out, int32_t** ptr_out, int32_t** items_out,
+                   cudaStream_t s) {
+    S->g = Grid{x, y, nx, ny};
+    S->ncx = nx - 1;
+    S->ncy = ny - 1;
+    S->blx = bbox_h[0];
+    S->bly = bbox_h[1];
+    S->bux = bbox_h[2];
+    S->buy = bbox_h[3];
+    S->nbound = 2 * (nx - 1) + 2 * (ny - 1);
+    int64_t nedges = 2 * S->ncy + 2 * S->ncx;
+    Edge* edges = nullptr;
+    RG_TRY(dalloc(&edges, (size_t)nedges, s));
+    *edges_out = edges;
+    boundary_edges_kernel<<<grid_for(nedges, 128), 128, 0, s>>>(S->g, edges, nedges);
+    S->edges = edges;
+    // bins: square, sized so that a bin holds about one edge along the boundary
+    double ex = S->bux - S->blx, ey = S->buy - S->bly;
+    double ext = ex > ey ? ex : ey;
+    int64_t side = nedges / 8;
+    if (side < 8) side = 8;
+    if (side > 1024) side = 1024;
+    double hbin = ext > 0 && std::isfinite(ext) ? ext / (double)side : 1.0;
+    Bins b;
+    b.ox = S->blx;
+    b.oy = S->bly;
+    b.inv_h = 1.0 / hbin;
+    b.nbx = (int)std::min<double>(1024.0, std::max(1.0, std::ceil(ex / hbin)));
+    b.nby = (int)std::min<double>(1024.0, std::max(1.0, std::ceil(ey / hbin)));
+    if (!std::isfinite(ex) || !std::isfinite(ey)) { b.nbx = 1; b.nby = 1; }
+    int64_t nbins = (int64_t)b.nbx * b.nby;
+    unsigned* counts = nullptr;
+    int64_t* ptr64 = nullptr;
+    int32_t *ptr32 = nullptr, *items = nullptr;
+    int64_t* total_dev = nullptr;
+    RG_TRY(dalloc(&counts, (size_t)nbins + 1, s));
+    RG_TRY(dalloc(&ptr64, (size_t)nbins + 1, s));
+    RG_TRY(dalloc(&ptr32, (size_t)nbins + 1, s));
+    RG_TRY(dalloc(&total_dev, 1, s));
+    RG_CUDA(cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbins + 1), s));
+    b.ptr = nullptr;
+    b.items = nullptr;
+    bin_edges_kernel<false><<<grid_for(nedges, 128), 128, 0, s>>>(edges, nedges, b, counts, nullptr,
+                                                                   nullptr);
+    RG_TRY(exclusive_scan_u32_to_i64(counts, ptr64, nbins + 1, total_dev, s));
+    int64_t total = 0;
+    RG_CUDA(cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    RG_CUDA(cudaStreamSynchronize(s));
+    RG_TRY(dalloc(&items, (size_t)total, s));
+    RG_CUDA(cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbins + 1), s));
+    bin_edges_kernel<true><<<grid_for(nedges, 128), 128, 0, s>>>(edges, nedges, b, counts, items,
+                                                                  ptr64);
+    i64_to_i32<<<grid_for(nbins + 1, 256), 256, 0, s>>>(ptr64, ptr32, nbins + 1);
+    RG_CUDA(cudaGetLastError());
+    dfree(counts, s);
+    dfree(ptr64, s);
+    dfree(total_dev, s);
+    b.ptr = ptr32;
+    b.items = items;
+    S->bins = b;
+    *ptr_out = ptr32;
+    *items_out = items;
+    return RG_OK;
+}
+
+}  // namespace
+
+int cell_area_2d(const double* x, const double* y, int64_t nx, int64_t ny, double* area,
+                 cudaStream_t s) {
+    int64_t n = (nx - 1) * (ny - 1);
+    if (n <= 0) return RG_OK;
+    cell_area_kernel<<<grid_for(n, 256), 256, 0, s>>>(x, y, nx, ny, area);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+// Seat lookup for points (the locator entry point): method 0 brute, 1 secant
+__global__ void locate_points_kernel(Grid g, const double* px, const double* py, int64_t n,
+                                     int method, int64_t* oi, int64_t* oj) {
+    int lane = threadIdx.x & 31;
+    int64_t k = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (k >= n) return;
+    double x = px[k], y = py[k];
+    int64_t i = MAXSIZE, j = MAXSIZE;
+    int ok = 0;
+    if (method == 1) {
+        if (lane == 0) ok = locate_secant(g, x, y, &i, &j);
+        ok = __shfl_sync(0xffffffffu, ok, 0);
+    }
+    if (!ok) locate_brute_warp(g, x, y, &i, &j);
+    if (lane == 0) {
+        oi[k] = i;
+        oj[k] = j;
+    }
+}
+
+int locate_2d_exact(const double* x, const double* y, int64_t nx, int64_t ny, const double* px,
+                    const double* py, int64_t n, int method, int64_t* oi, int64_t* oj,
+                    cudaStream_t s) {
+    if (n <= 0) return RG_OK;
+    locate_points_kernel<<<grid_for(n * 32, 128), 128, 0, s>>>(Grid{x, y, nx, ny}, px, py, n, method,
+                                                               oi, oj);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64_t nyi,
+                          const double* xo, const double* yo, int64_t nxo, int64_t nyo,
+                          const double* w_in, cudaStream_t s, rg_weights_s* W) {
+    RG_CHECK(nxi >= 2 && nyi >= 2 && nxo >= 2 && nyo >= 2, RG_ERR_ARG,
+             "conservative 2D grids need at least 2 vertices per axis");
+    int64_t ncx_in = nxi - 1, ncy_in = nyi - 1, ncx_out = nxo - 1, ncy_out = nyo - 1;
+    int64_t n_in = ncx_in * ncy_in, n_out = ncx_out * ncy_out;
+    RG_CHECK(n_in < INT32_MAX && n_out < INT32_MAX, RG_ERR_UNSUPPORTED,
+             "grids above 2^31 cells are not supported");
+
+    int st = RG_OK;
+    double* area_in = nullptr;
+    double* bbox_d = nullptr;
+    Edge* edges[2] = {nullptr, nullptr};
+    int32_t* bptr[2] = {nullptr, nullptr};
+    int32_t* bitems[2] = {nullptr, nullptr};
+    Seat* seats = nullptr;
+    int64_t *counts = nullptr, *offsets = nullptr, *total_dev = nullptr;
+    unsigned* flags = nullptr;
+    int32_t *raw_in = nullptr, *raw_out = nullptr;
+    double* raw_val = nullptr;
+    int64_t* skey = nullptr;
+    int64_t* bucket_ptr = nullptr;
+    uint32_t* perm = nullptr;
+    int32_t* tmp_col = nullptr;
+    double* tmp_val = nullptr;
+    int64_t* row_nnz = nullptr;
+
+    do {
+        if ((st = dalloc(&area_in, (size_t)n_in, s))) break;
+        if ((st = cell_area_2d(xi, yi, nxi, nyi, area_in, s))) break;
+        if ((st = dalloc(&bbox_d, 8, s))) break;
+        if ((st = dalloc(&flags, 1, s))) break;
+        if ((st = dalloc(&total_dev, 1, s))) break;
+        cudaMemsetAsync(flags, 0, sizeof(unsigned), s);
+        bbox_kernel<<<1, 256, 0, s>>>(xi, yi, nxi * nyi, bbox_d);
+        bbox_kernel<<<1, 256, 0, s>>>(xo, yo, nxo * nyo, bbox_d + 4);
+        double bbox_h[8];
+        cudaMemcpyAsync(bbox_h, bbox_d, sizeof(bbox_h), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("build_conservative_2d: %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+
+        SweepParams P;
+        memset(&P, 0, sizeof(P));
+        if ((st = prepare_static(xi, yi, nxi, nyi, bbox_h, &P.st[0], &edges[0], &bptr[0], &bitems[0], s)))
+            break;
+        if ((st = prepare_static(xo, yo, nxo, nyo, bbox_h + 4, &P.st[1], &edges[1], &bptr[1], &bitems[1],
+                                 s)))
+            break;
+        // families in upstream order: sweep output (axis 0, 1), sweep input (axis 0, 1)
+        int64_t base = 0;
+        for (int k = 0; k < 4; k++) {
+            Family& F = P.fam[k];
+            F.sweep_input = k >= 2;
+            F.axis = k & 1;
+            F.sweep = F.sweep_input ? Grid{xi, yi, nxi, nyi} : Grid{xo, yo, nxo, nyo};
+            F.st = F.sweep_input ? 1 : 0;
+            F.transposed = F.axis == 0;
+            F.lines = F.axis == 0 ? F.sweep.ny : F.sweep.nx;
+            F.len = F.axis == 0 ? F.sweep.nx : F.sweep.ny;
+            F.line_base = base;
+            base += F.lines;
+        }
+        P.total_lines = base;
+        P.area_in = area_in;
+        P.w_in = w_in;
+        P.ncy_in = ncy_in;
+        P.ncy_out = ncy_out;
+
+        if ((st = dalloc(&seats, (size_t)base, s))) break;
+        if ((st = dalloc(&counts, (size_t)base + 1, s))) break;
+        if ((st = dalloc(&offsets, (size_t)base + 1, s))) break;
+        seat_kernel<<<grid_for(base * 32, 128), 128, 0, s>>>(P, seats, flags);
+        walk_kernel<false><<<grid_for(base, 64), 64, 0, s>>>(P, seats, counts, nullptr, nullptr, nullptr,
+                                                             nullptr, flags);
+        if ((st = exclusive_scan_i64(counts, offsets, base, total_dev, s))) break;
+        int64_t nraw = 0;
+        unsigned fl = 0;
+        cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("build_conservative_2d (count walk): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        if (fl & (FLAG_WALK_CAP | FLAG_SEAT_OUTSIDE)) {
+            set_error("conservative sweep: %s",
+                      (fl & FLAG_WALK_CAP) ? "a grid line exceeded its step cap (degenerate grids?)"
+                                           : "a grid line starting inside the grid boundary could "
+                                             "not be located in any cell");
+            st = RG_ERR_WALK;
+            break;
+        }
+        if (nraw >= (int64_t)UINT32_MAX) {
+            set_error("conservative sweep: %lld raw entries exceed 2^32", (long long)nraw);
+            st = RG_ERR_UNSUPPORTED;
+            break;
+        }
+        if ((st = dalloc(&raw_in, (size_t)nraw, s))) break;
+        if ((st = dalloc(&raw_out, (size_t)nraw, s))) break;
+        if ((st = dalloc(&raw_val, (size_t)nraw, s))) break;
+        walk_kernel<true><<<grid_for(base, 64), 64, 0, s>>>(P, seats, nullptr, offsets, raw_in, raw_out,
+                                                            raw_val, flags);
+        // merge
+        if ((st = dalloc(&skey, (size_t)nraw, s))) break;
+        if ((st = dalloc(&bucket_ptr, (size_t)n_out + 1, s))) break;
+        if ((st = dalloc(&perm, (size_t)nraw, s))) break;
+        if (nraw > 0) make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(
+            raw_in, nraw, skey);
+        if ((st = bucket_sort(raw_out, skey, nraw, n_out, bucket_ptr, perm, flags, s))) break;
+        dfree(skey, s);
+        skey = nullptr;
+        if ((st = dalloc(&tmp_col, (size_t)nraw, s))) break;
+        if ((st = dalloc(&tmp_val, (size_t)nraw, s))) break;
+        if ((st = dalloc(&row_nnz, (size_t)n_out + 1, s))) break;
+        merge_rows<<<grid_for(n_out, 128), 128, 0, s>>>(bucket_ptr, perm, raw_in, raw_val, n_out, tmp_col,
+                                                        tmp_val, row_nnz);
+        if ((st = dalloc(&W->row_ptr, (size_t)n_out + 1, s))) break;
+        if ((st = exclusive_scan_i64(row_nnz, W->row_ptr, n_out + 1, total_dev, s))) break;
+        int64_t nnz = 0;
+        cudaMemcpyAsync(&nnz, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("build_conservative_2d (merge): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        if ((st = dalloc(&W->col, (size_t)nnz, s))) break;
+        if ((st = dalloc(&W->val, (size_t)nnz, s))) break;
+        compact_rows<<<grid_for(n_out, 128), 128, 0, s>>>(bucket_ptr, W->row_ptr, tmp_col, tmp_val, n_out,
+                                                          W->col, W->val);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("build_conservative_2d: %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        W->n_in = n_in;
+        W->n_out = n_out;
+        W->nnz = nnz;
+        W->out_shape0 = ncx_out;
+        W->out_shape1 = ncy_out;
+    } while (0);
+
+    dfree(area_in, s);
+    dfree(bbox_d, s);
+    for (int k = 0; k < 2; k++) {
+        dfree(edges[k], s);
+        dfree(bptr[k], s);
+        dfree(bitems[k], s);
+    }
+    dfree(seats, s);
+    dfree(counts, s);
+    dfree(offsets, s);
+    dfree(total_dev, s);
+    dfree(flags, s);
+    dfree(raw_in, s);
+    dfree(raw_out, s);
+    dfree(raw_val, s);
+    dfree(skey, s);
+    dfree(bucket_ptr, s);
+    dfree(perm, s);
+    dfree(tmp_col, s);
+    dfree(tmp_val, s);
+    dfree(row_nnz, s);
+    return st;
+}
+
+}  // namespace rg

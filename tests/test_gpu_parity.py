@@ -1,0 +1,383 @@
+"""GPU parity: the CUDA path against the upstream's own outputs (golden
+fixtures) and against the CPU oracle at sizes the fixtures do not reach.
+
+Tolerances: indices and weights are compared bit for bit (the kernels follow
+the upstream arithmetic exactly); exact-mode applies are bit for bit; the
+float32 fast apply is checked to 1e-6 relative.
+"""
+
+import numpy as np
+import pytest
+
+import fixtures
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+KNOWN = fixtures.load("known_answers.npz")
+ONE = fixtures.load("one_dim.npz")
+CURVI = fixtures.load("curvilinear.npz")
+
+
+@pytest.fixture(scope="module")
+def rg():
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import regridding_gb300
+
+    return regridding_gb300
+
+
+def assert_same(a, b):
+    a = np.asarray(a)
+    b = np.asarray(b)
+    assert a.shape == b.shape, (a.shape, b.shape)
+    assert np.array_equal(a, b, equal_nan=True), np.max(np.abs(a - b)) if a.dtype.kind == "f" else None
+
+
+def assert_weights_same(got, exp):
+    ga, gs_in, gs_out = got
+    ea, es_in, es_out = exp
+    assert tuple(gs_in) == tuple(es_in) and tuple(gs_out) == tuple(es_out)
+    assert ga.shape == ea.shape
+    for g, e in zip(ga.reshape(-1), ea.reshape(-1)):
+        for x, y in zip(g, e):
+            assert_same(x, y)
+
+
+def kw_axes(meta):
+    out = {}
+    for k in ("axis_input", "axis_output"):
+        v = meta.get(k)
+        out[k] = tuple(v) if isinstance(v, list) else v
+    return out
+
+
+# ---------------------------------------------------------------------------
+# conservative 2D known answers
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("k", range(15))
+def test_conservative_2d_known_answers(rg, k):
+    c = KNOWN.case(f"c2d_{k}")
+    wi = c["weights_input"] if c.has("weights_input") else None
+    w = rg.weights(c.tuple("ci"), c.tuple("co"), weights_input=wi, method="conservative", perturb=False)
+    assert_weights_same(w, c.weights())
+    res = rg.regrid_from_weights(*w, values_input=c["values_input"])
+    assert_same(res, c["result"])
+    assert np.allclose(res, c["expected"], rtol=1e-3)
+
+
+def test_saved_layout_contract(rg):
+    c = KNOWN.case("layout")
+    ci, co = c.tuple("ci"), c.tuple("co")
+    w = rg.weights(ci, co, method="conservative")
+    assert_weights_same(w, c.weights())
+    for ii, oo, vv in w[0].reshape(-1):
+        assert ii.dtype == np.int64 and oo.dtype == np.int64 and vv.dtype == np.float64
+        key = ii * (oo.max() + 1) + oo
+        assert np.unique(key).size == key.size
+    vals = c["values_input"]
+    assert_same(rg.regrid_from_weights(*w, values_input=vals), c["result"])
+    assert_same(rg.regrid(ci, co, values_input=vals, method="conservative"), c["result"])
+    assert_same(rg.regrid(ci, co, values_input=vals, method="conservative"), c["regrid"])
+    # pickle round trip gives a bit-identical apply
+    import pickle
+
+    w2 = pickle.loads(pickle.dumps(w))
+    assert_same(rg.regrid_from_weights(*w2, values_input=vals), c["result"])
+    # transposes
+    wt = rg.transpose_weights(w)
+    assert wt[1] == w[2] and wt[2] == w[1]
+    for t_el, el in zip(wt[0].reshape(-1), w[0].reshape(-1)):
+        assert t_el[0] is el[1] and t_el[1] is el[0] and t_el[2] is el[2]
+    wtc = rg.transpose_weights_conservative(w, ci, co)
+    assert_weights_same(wtc, c.weights("transposed_conservative"))
+    back = rg.regrid_from_weights(*wtc, values_input=rg.regrid_from_weights(*w, values_input=vals))
+    assert_same(back, c["roundtrip"])
+
+
+@pytest.mark.parametrize("tag", ["default", "s12345", "s0", "s1", "gen12345", "unperturbed"])
+def test_seeded_perturbation(rg, tag):
+    c = KNOWN.case("seed")
+    kw = {"default": {}, "s12345": {"seed": 12345}, "s0": {"seed": 0}, "s1": {"seed": 1},
+          "gen12345": {"seed": np.random.default_rng(12345)}, "unperturbed": {"perturb": False}}[tag]
+    w = rg.weights(c.tuple("ci"), c.tuple("co"), method="conservative", **kw)
+    assert_weights_same(w, c.weights(f"w_{tag}"))
+
+
+def test_transpose_orthogonal_axis(rg):
+    c = KNOWN.case("tw_orth")
+    ci, co = c.tuple("ci"), c.tuple("co")
+    w = rg.weights(ci, co, axis_input=(0, 1), axis_output=(0, 1), method="conservative")
+    assert_weights_same(w, c.weights())
+    data = rg.regrid_from_weights(*w, values_input=c["values_input"], axis_input=(0, 1), axis_output=(0, 1))
+    assert_same(data, c["data"])
+    back = rg.regrid_from_weights(*rg.transpose_weights(w), values_input=data, axis_input=(0, 1),
+                                  axis_output=(0, 1))
+    assert_same(back, c["back"])
+
+
+@pytest.mark.parametrize("k", range(4))
+def test_transpose_conservative(rg, k):
+    c = KNOWN.case(f"twc_{k}")
+    ci, co = c.tuple("ci"), c.tuple("co")
+    ai, ao, wi = c.meta["axis_input"], c.meta["axis_output"], c.meta["weights_input"]
+    if len(ci) == 1:
+        ci, co = ci[0], co[0]
+    w = rg.weights(ci, co, axis_input=ai, axis_output=ao, weights_input=wi, method="conservative")
+    assert_weights_same(w, c.weights())
+    wtc = rg.transpose_weights_conservative(w, ci, co, axis_input=ai, axis_output=ao, weights_input=wi)
+    assert_weights_same(wtc, c.weights("transposed"))
+    vals = rg.regrid_from_weights(*wtc, values_input=np.array(10), axis_input=ai, axis_output=ao)
+    assert_same(vals, c["values"])
+
+
+def test_transpose_conservative_inverts_weights_input_2d(rg):
+    c = KNOWN.case("twc_inv2d")
+    ci, co, wi = c.tuple("ci"), c.tuple("co"), c["weights_input"]
+    w = rg.weights(ci, co, weights_input=wi, method="conservative", perturb=False)
+    assert_weights_same(w, c.weights())
+    wtc = rg.transpose_weights_conservative(w, ci, co, weights_input=wi)
+    assert_weights_same(wtc, c.weights("transposed"))
+    rt = rg.regrid_from_weights(*wtc, values_input=rg.regrid_from_weights(*w, values_input=c["values"]))
+    assert_same(rt, c["roundtrip"])
+
+
+# ---------------------------------------------------------------------------
+# 1D
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("k", range(7))
+def test_multilinear_known_answers(rg, k):
+    c = ONE.case(f"ml_{k}")
+    kw = kw_axes(c.meta)
+    ci, co = c.tuple("ci"), c.tuple("co")
+    w = rg.weights(ci, co, weights_input=c.meta["weights_input"], method="multilinear", **kw)
+    assert_weights_same(w, c.weights())
+    vo = np.empty(shape=11) if c.meta["values_output"] else None
+    res = rg.regrid_from_weights(*w, values_input=c["values_input"], values_output=vo, **kw)
+    assert res.dtype == np.float64
+    assert_same(res, c["result"])
+
+
+def test_multilinear_bounds(rg):
+    c = ONE.case("bounds")
+    x, xo = c["x"], c["x_output"]
+    for b in ("extrapolate", "nan"):
+        w = rg.weights((x,), (xo,), method="multilinear", bounds=b)
+        assert_weights_same(w, c.weights(f"weights_{b}"))
+        res = rg.regrid((x,), (xo,), values_input=c["values"], method="multilinear", bounds=b)
+        assert_same(res, c[f"result_{b}"])
+    with pytest.raises(ValueError, match="fall outside the input grid"):
+        rg.regrid((x,), (xo,), values_input=c["values"], method="multilinear", bounds="raise")
+    inside = rg.regrid((x,), (np.array([0.5, 3.5]),), values_input=c["values"], method="multilinear",
+                       bounds="raise")
+    assert np.allclose(inside, [0.5, 12.5])
+    with pytest.raises(ValueError, match="Unrecognized bounds="):
+        rg.regrid((x,), (xo,), values_input=c["values"], method="multilinear", bounds="foo")
+
+
+@pytest.mark.parametrize("k", range(13))
+def test_conservative_1d_known_answers(rg, k):
+    c = ONE.case(f"c1d_{k}")
+    ai, ao = c.meta["axis_input"], c.meta["axis_output"]
+    ai = tuple(ai) if isinstance(ai, list) else ai
+    ao = tuple(ao) if isinstance(ao, list) else ao
+    wi = c["weights_input"] if c.has("weights_input") else None
+    w = rg.weights(c["ci"], c["co"], axis_input=ai, axis_output=ao, weights_input=wi, method="conservative")
+    assert_weights_same(w, c.weights())
+    res = rg.regrid_from_weights(*w, values_input=c["values_input"], axis_input=ai, axis_output=ao)
+    assert_same(res, c["result"])
+
+
+@pytest.mark.parametrize("name", ["fi_0", "fi_1", "fi_2", "fi_3", "fi_4"])
+def test_find_indices_1d(rg, name):
+    c = ONE.case(name)
+    for method in ("brute", "searchsorted"):
+        (got,) = rg.find_indices((c["ci"],), (c["co"],), method=method, fill_value=c.meta["fill_value"])
+        assert_same(got, c[f"result_{method}"])
+    with pytest.raises(ValueError):
+        rg.find_indices((c["ci"],), (c["co"],), method="invalid method")
+
+
+def test_find_indices_1d_batched_against_oracle(rg):
+    rng = np.random.default_rng(7)
+    xi = np.sort(rng.uniform(0, 1, (40, 300)), axis=-1)
+    xi[3] = xi[3][::-1]  # a descending row: brute scans it linearly
+    xo = rng.uniform(-0.05, 1.05, (40, 500))
+    xo[5, :7] = xi[5, :7]  # points exactly on vertices
+    for method in ("brute", "searchsorted"):
+        (got,) = rg.find_indices((xi,), (xo,), axis_input=-1, axis_output=-1, method=method)
+        exp = oracle.find_indices_1d(xi, xo, method=method)
+        if method == "searchsorted":
+            # searchsorted is only defined on ascending rows
+            got, exp = np.delete(got, 3, axis=0), np.delete(exp, 3, axis=0)
+        assert_same(got, exp)
+
+
+# ---------------------------------------------------------------------------
+# 2D point location
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("k", range(6))
+def test_locate_known_answers(rg, k):
+    c = KNOWN.case(f"loc_{k}")
+    g = c.tuple("grid")
+    p = c["point"]
+    for method, key in (("exhaustive", "brute"), ("secant", "secant"), ("brute", "brute")):
+        oi, oj = rg.locate_2d(g, p[:1], p[1:], method=method)
+        assert (int(oi[0]), int(oj[0])) == tuple(int(v) for v in c[key]), method
+
+
+def test_locate_against_oracle(rg):
+    c = CURVI.case("curvi129")
+    g = c.tuple("ci")
+    rng = np.random.default_rng(3)
+    px = rng.uniform(-1.3, 1.3, 4000)
+    py = rng.uniform(-1.3, 1.3, 4000)
+    # points on vertices and edge midpoints of the grid
+    px[:50] = g[0][5:55, 7]
+    py[:50] = g[1][5:55, 7]
+    px[50:100] = 0.5 * (g[0][10, 3:53] + g[0][10, 4:54])
+    py[50:100] = 0.5 * (g[1][10, 3:53] + g[1][10, 4:54])
+    exp = oracle.locate(g, px, py, "brute")
+    for method in ("brute", "exhaustive"):
+        got = rg.locate_2d(g, px, py, method=method)
+        assert_same(got[0], exp[0])
+        assert_same(got[1], exp[1])
+    got = rg.locate_2d(g, px, py, method="secant")
+    exp = oracle.locate(g, px, py, "secant")
+    assert_same(got[0], exp[0])
+    assert_same(got[1], exp[1])
+
+
+def test_find_indices_2d_extension(rg):
+    c = CURVI.case("curvi33")
+    gi, go = c.tuple("ci"), c.tuple("co")
+    i, j = rg.find_indices(gi, go)
+    exp = oracle.locate(gi, go[0].ravel(), go[1].ravel(), "brute")
+    fill = np.iinfo(np.int64).max
+    assert_same(i.ravel(), np.where(exp[0] == fill, fill, exp[0]))
+    assert_same(j.ravel(), exp[1])
+    with pytest.raises(ValueError):
+        rg.find_indices(gi, go, method="searchsorted")
+
+
+# ---------------------------------------------------------------------------
+# benchmark-shaped grids
+# ---------------------------------------------------------------------------
+
+
+@pytest.mark.parametrize("name", ["cfg1", "curvi33", "curvi129"])
+def test_curvilinear_weights_bit_exact(rg, name):
+    c = CURVI.case(name)
+    w = rg.weights(c.tuple("ci"), c.tuple("co"), method="conservative")
+    assert_weights_same(w, c.weights())
+
+
+def test_cfg1_apply(rg):
+    c = CURVI.case("cfg1")
+    w = rg.weights(c.tuple("ci"), c.tuple("co"), method="conservative")
+    res = rg.regrid_from_weights(*w, values_input=c["values_input"])
+    assert_same(res, c["result"])
+    assert_same(rg.regrid(c.tuple("ci"), c.tuple("co"), values_input=c["values_input"], method="conservative"),
+                c["result"])
+    f32 = c["values_input"].astype(np.float32)
+    fast = rg.regrid_from_weights(*w, values_input=f32, accumulate="fast")
+    assert fast.dtype == np.float32
+    np.testing.assert_allclose(fast, c["result"], rtol=1e-6, atol=1e-6 * np.abs(c["result"]).max())
+    # the upstream in-place float32 output
+    out32 = np.empty((8, 48, 48), dtype=np.float32)
+    rg.regrid_from_weights(*w, values_input=f32, values_output=out32)
+    (ii, oo, vv), = w[0].reshape(-1)
+    exp32 = np.empty((8, 48 * 48), dtype=np.float32)
+    oracle.apply(ii, oo, vv, f32.reshape(8, -1), 48 * 48, values_output=exp32)
+    assert_same(out32.reshape(8, -1), exp32)
+    swapped = rg.weights(c.tuple("co"), c.tuple("ci"), weights_input=np.linspace(0.5, 2, 48 * 48).reshape(48, 48),
+                         method="conservative")
+    (si, so, sv), = swapped[0].reshape(-1)
+    assert si.size > 0 and np.all(sv[np.abs(sv) > 1e-12] > 0)
+
+
+def distorted(n, angle, amp, lo=-1.0, hi=1.0):
+    a = np.linspace(lo, hi, n)
+    x, y = np.meshgrid(a, a, indexing="ij")
+    xr = x * np.cos(angle) - y * np.sin(angle)
+    yr = x * np.sin(angle) + y * np.cos(angle)
+    xr = xr + amp * np.sin(np.pi * yr)
+    yr = yr + amp * np.sin(np.pi * xr)
+    return xr, yr
+
+
+def rect(n, lo, hi):
+    a = np.linspace(lo, hi, n)
+    return tuple(np.meshgrid(a, a, indexing="ij"))
+
+
+@pytest.mark.parametrize("n_in,n_out,angle", [(257, 193, 0.25), (513, 385, 0.4), (200, 301, 0.1)])
+def test_weights_against_oracle(rg, n_in, n_out, angle):
+    gi = distorted(n_in, angle, 0.02)
+    go = rect(n_out, -1.05, 1.05)
+    rng = np.random.default_rng(42)
+    gop = tuple(rng.normal(a, np.ptp(a) * 1e-9) for a in go)
+    exp = oracle.weights_conservative_2d(gi, gop)
+    dw = rg.build_conservative_2d(gi, gop)
+    got = dw.export_numpy()
+    for g, e in zip(got, exp):
+        assert_same(g, e)
+    # apply: exact float64 bit for bit, fast float32 within 1e-6
+    import torch
+
+    vals = rng.lognormal(3, 1, (16, n_in - 1, n_in - 1)).astype(np.float32)
+    ref = oracle.apply(exp[0], exp[1], exp[2], vals.reshape(16, -1), (n_out - 1) ** 2)
+    d_vals = torch.from_numpy(vals.reshape(16, -1)).cuda()
+    exact = dw.apply(d_vals).cpu().numpy()
+    assert_same(exact, ref)
+    fast = dw.apply(d_vals, accumulate="fast").cpu().numpy()
+    assert fast.dtype == np.float32
+    np.testing.assert_allclose(fast, ref, rtol=1e-6, atol=1e-6 * ref.max())
+    # transposed apply against the oracle with swapped indices
+    back = dw.apply(torch.from_numpy(ref).cuda(), transpose=True).cpu().numpy()
+    ref_t = oracle.apply(exp[1], exp[0], exp[2], ref, (n_in - 1) ** 2)
+    np.testing.assert_allclose(back, ref_t, rtol=1e-12, atol=1e-12 * np.abs(ref_t).max())
+
+
+def test_build_is_deterministic(rg):
+    gi = distorted(301, 0.3, 0.03)
+    go = rect(257, -1.1, 1.1)
+    a = rg.build_conservative_2d(gi, go).export_numpy()
+    b = rg.build_conservative_2d(gi, go).export_numpy()
+    for x, y in zip(a, b):
+        assert_same(x, y)
+
+
+def test_large_grid_properties(rg):
+    """2048^2 -> 1536^2: size-independent checks (conservation, bounds, symmetry of roles)."""
+    import torch
+
+    gi = distorted(2049, 0.3, 0.02)
+    go = rect(1537, -1.05, 1.05)
+    dw = rg.build_conservative_2d(gi, go)
+    ii, oo, vv = dw.export_numpy()
+    assert np.all(np.diff(ii) >= 0)
+    area_in = rg.cell_volume(gi, (0, 1)).reshape(-1)
+    area_out = rg.cell_volume(go, (0, 1)).reshape(-1)
+    overlap = np.bincount(oo, weights=vv * area_in[ii], minlength=area_out.size)
+    # each output cell is covered at most once (to rounding of the cancelling sums)
+    assert np.all(overlap <= area_out * (1 + 1e-9) + 1e-15)
+    # each input cell distributes at most all of itself
+    frac = np.bincount(ii, weights=vv, minlength=area_in.size)
+    assert np.all(frac <= 1 + 1e-9)
+    # interior input cells are fully covered by the larger output grid
+    inner = frac.reshape(2048, 2048)[200:-200, 200:-200]
+    np.testing.assert_allclose(inner, 1.0, rtol=0, atol=1e-9)
+    # apply conserves the covered flux
+    vals = torch.ones((2, 2048 * 2048), dtype=torch.float32, device="cuda")
+    out = dw.apply(vals).cpu().numpy()
+    np.testing.assert_allclose(out[0].sum(), frac.sum(), rtol=1e-9)
+    assert frac.sum() > 0.9 * 2048 * 2048

@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import ctypes
 import threading
+import warnings
 import weakref
 
 import numpy as np
@@ -41,7 +42,12 @@ def upload(a: np.ndarray, dtype=None):
     """Host array -> contiguous CUDA tensor (pinned staging for large arrays)."""
     t = torch()
     a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
-    host = t.from_numpy(a) if a.dtype != np.bool_ else t.from_numpy(a.astype(np.uint8))
+    if a.dtype == np.bool_:
+        a = a.astype(np.uint8)
+    with warnings.catch_warnings():
+        # read-only arrays (the saved weights) are only read from
+        warnings.simplefilter("ignore", UserWarning)
+        host = t.from_numpy(a)
     if a.nbytes >= (1 << 20):
         host = host.pin_memory()
         return host.to("cuda", non_blocking=True)

@@ -36,6 +36,10 @@ def find_indices(
     if fill_value is None:
         fill_value = np.iinfo(int).max
 
+    if len(axi) == 2:
+        # 2D: keep the resampled axes in ascending order, so (i, j) index the
+        # grid as stored (the upstream has no 2D search to follow here)
+        axi, axo = tuple(sorted(axi)), tuple(sorted(axo))
     numba_in = _util.numba_axes(len(axi))
     numba_out = _util.numba_axes(len(axo))
     shape_in_numba = tuple(shape_in[ax] for ax in axi)

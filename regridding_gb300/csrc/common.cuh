@@ -73,6 +73,7 @@ int dalloc(T** p, size_t n, cudaStream_t s) {
     if (n == 0) n = 1;
     cudaError_t e = cudaMallocAsync((void**)p, n * sizeof(T), s);
     if (e != cudaSuccess) {
+        cudaGetLastError();  // a failed allocation must not leave a sticky error for later checks
         set_error("cudaMallocAsync(%zu bytes): %s", n * sizeof(T), cudaGetErrorString(e));
         return RG_ERR_ALLOC;
     }

@@ -451,10 +451,15 @@ __global__ void __launch_bounds__(128) seat_kernel(SweepParams P, Seat* seats, u
             if (lane == 0) ok = locate_secant(S.g, x1, y1, &i, &j);
             ok = __shfl_sync(0xffffffffu, ok, 0);
             if (!ok) locate_brute_warp(S.g, x1, y1, &i, &j);
-            seat.stx = i;
-            seat.sty = j;
-            seat.outside = 0;
-            if (i == MAXSIZE) atomicOr(flags, FLAG_SEAT_OUTSIDE);
+            if (i == MAXSIZE) {
+                // the upstream would index out of range here; report it and
+                // leave the line outside so the walk stays in bounds
+                if (lane == 0) atomicOr(flags, FLAG_SEAT_OUTSIDE);
+            } else {
+                seat.stx = i;
+                seat.sty = j;
+                seat.outside = 0;
+            }
         }
     }
     if (lane == 0) seats[line] = seat;
@@ -491,6 +496,7 @@ __global__ void __launch_bounds__(64)
     int64_t sy_idx = 0;
     int64_t n_emit = 0;
     int64_t wpos = WRITE ? offsets[line] : 0;
+    const int64_t wend = WRITE ? offsets[line + 1] : 0;
     const int64_t max_steps = 64 * (F.len + 4 * (S.ncx + S.ncy) + 16);
     int64_t steps = 0;
     double x1 = F.SX(li, 0), y1 = F.SY(li, 0);
@@ -598,6 +604,10 @@ __global__ void __launch_bounds__(64)
                 else { ii = stx; ij = sty; oi = a; oj = b; }
                 int64_t in_flat = ii * P.ncy_in + ij;
                 if (WRITE) {
+                    if (wpos >= wend) {  // the count walk disagreed: never write past the line's slots
+                        atomicOr(flags, FLAG_CAPACITY);
+                        continue;
+                    }
                     double ain = __ldg(P.area_in + in_flat);
                     double w = side == 0 ? ddiv(area, ain) : ddiv(-area, ain);
                     if (P.w_in) w = dmul(w, __ldg(P.w_in + in_flat));
@@ -929,7 +939,8 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
         seat_kernel<<<grid_for(base * 32, 128), 128, 0, s>>>(P, seats, flags);
         walk_kernel<false><<<grid_for(base, 64), 64, 0, s>>>(P, seats, counts, nullptr, nullptr, nullptr,
                                                              nullptr, flags);
-        if ((st = exclusive_scan_i64(counts, offsets, base, total_dev, s))) break;
+        cudaMemsetAsync(counts + base, 0, sizeof(int64_t), s);
+        if ((st = exclusive_scan_i64(counts, offsets, base + 1, total_dev, s))) break;
         int64_t nraw = 0;
         unsigned fl = 0;
         cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
@@ -960,6 +971,7 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
                                                             raw_val, flags);
         // merge
         if ((st = dalloc(&skey, (size_t)nraw, s))) break;
+        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         if ((st = dalloc(&bucket_ptr, (size_t)n_out + 1, s))) break;
         if ((st = dalloc(&perm, (size_t)nraw, s))) break;
         if (nraw > 0) make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(
@@ -970,6 +982,7 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
         if ((st = dalloc(&tmp_col, (size_t)nraw, s))) break;
         if ((st = dalloc(&tmp_val, (size_t)nraw, s))) break;
         if ((st = dalloc(&row_nnz, (size_t)n_out + 1, s))) break;
+        cudaMemsetAsync(row_nnz + n_out, 0, sizeof(int64_t), s);
         merge_rows<<<grid_for(n_out, 128), 128, 0, s>>>(bucket_ptr, perm, raw_in, raw_val, n_out, tmp_col,
                                                         tmp_val, row_nnz);
         if ((st = dalloc(&W->row_ptr, (size_t)n_out + 1, s))) break;
@@ -980,6 +993,11 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
         if (e != cudaSuccess) {
             set_error("build_conservative_2d (merge): %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
+            break;
+        }
+        if (fl & FLAG_CAPACITY) {
+            set_error("conservative sweep: the write walk disagreed with the count walk");
+            st = RG_ERR_WALK;
             break;
         }
         if ((st = dalloc(&W->col, (size_t)nnz, s))) break;

@@ -301,6 +301,10 @@ __global__ void transpose_scale_kernel(const int64_t* __restrict__ ii, const int
          k += (int64_t)gridDim.x * blockDim.x) {
         int64_t i = ii[k] < 0 ? ii[k] + n_in : ii[k];
         int64_t o = oo[k] < 0 ? oo[k] + n_out : oo[k];
+        if (i < 0 || i >= n_in || o < 0 || o >= n_out) {
+            res[k] = NAN;  // index outside the grids: no volume to scale by
+            continue;
+        }
         double x = v[k];
         if (w_in) {
             double wi = w_in[i];

@@ -349,7 +349,8 @@ def test_weights_against_oracle(rg, n_in, n_out, angle):
 
 def test_build_is_deterministic(rg):
     gi = distorted(301, 0.3, 0.03)
-    go = rect(257, -1.1, 1.1)
+    rng = np.random.default_rng(5)
+    go = tuple(rng.normal(a, np.ptp(a) * 1e-9) for a in rect(257, -1.1, 1.1))
     a = rg.build_conservative_2d(gi, go).export_numpy()
     b = rg.build_conservative_2d(gi, go).export_numpy()
     for x, y in zip(a, b):
@@ -362,6 +363,8 @@ def test_large_grid_properties(rg):
 
     gi = distorted(2049, 0.3, 0.02)
     go = rect(1537, -1.05, 1.05)
+    rng = np.random.default_rng(42)
+    go = tuple(rng.normal(a, np.ptp(a) * 1e-9) for a in go)
     dw = rg.build_conservative_2d(gi, go)
     ii, oo, vv = dw.export_numpy()
     assert np.all(np.diff(ii) >= 0)
@@ -381,3 +384,19 @@ def test_large_grid_properties(rg):
     out = dw.apply(vals).cpu().numpy()
     np.testing.assert_allclose(out[0].sum(), frac.sum(), rtol=1e-9)
     assert frac.sum() > 0.9 * 2048 * 2048
+
+
+def test_degenerate_grids_report_walk_error(rg):
+    """Exactly coincident input and output vertices without the default
+    perturbation make the upstream walk cycle forever; the oracle and the
+    GPU both stop at their step caps and report it."""
+    gi = distorted(65, 0.3, 0.02)
+    go = rect(49, -1.05, 1.05)
+    with pytest.raises(RuntimeError):
+        oracle.sweep_2d(gi, go)
+    with pytest.raises(rg.RegridError, match="step cap"):
+        rg.build_conservative_2d(gi, go)
+    # the library stays usable afterwards
+    rng = np.random.default_rng(42)
+    gop = tuple(rng.normal(a, np.ptp(a) * 1e-9) for a in go)
+    assert rg.build_conservative_2d(gi, gop).nnz > 0

@@ -157,3 +157,15 @@ def test_reduceat_model_matches_numpy():
         exp = np.add.reduceat(a, [0])[0]
         got = a[0] + pw(list(a[1:]))
         assert got == exp
+
+
+def test_degenerate_grids_hit_the_step_cap():
+    """Coincident vertices without perturbation: the upstream walk never ends;
+    the oracle stops at its step cap and reports an error instead."""
+    a = np.linspace(-1, 1, 17)
+    x, y = np.meshgrid(a, a, indexing="ij")
+    xr, yr = x * np.cos(0.3) - y * np.sin(0.3), x * np.sin(0.3) + y * np.cos(0.3)
+    b = np.linspace(-1.05, 1.05, 13)
+    xo, yo = np.meshgrid(b, b, indexing="ij")
+    with pytest.raises(RuntimeError, match="status 2"):
+        oracle.sweep_2d((xr, yr), (xo, yo))

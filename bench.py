@@ -1,0 +1,444 @@
+"""Benchmark of the regridding hot path on the 2048^2 -> 1536^2 workload.
+
+One step is one apply of saved conservative weights to a 64-deep float32
+stack (64 x 2048 x 2048 -> 64 x 1536 x 1536), the operation a user repeats
+for every array regridded between the same two grids.  ``value`` is the
+apply's algorithmic HBM traffic divided by its time (inputs resident in HBM;
+the 1.07 GB input stack is 8x the L2, so no flush is needed between steps).
+The same line reports the weight build (cells/s), the 2D find_indices over
+the output vertices, the exact float64-output apply, the end-to-end apply
+through the C ABI from host memory, and the CPU baseline (the C restatement
+of the upstream loops on every host core).
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+With N > 1 (torchrun, one process per GPU) every rank runs an independent
+replica of the workload; ``value`` sums the ranks' bytes over the slowest
+rank's time.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "build cells/s; apply HBM GB/s; served req/s + p50/p99 vs plain GPU path"
+STACK = 64
+N_IN = 2049
+N_OUT = 1537
+PEAK_FALLBACK_GBS = 6800.0
+
+
+# ---------------------------------------------------------------------------
+# workload bytes
+# ---------------------------------------------------------------------------
+
+
+def apply_bytes(stack: int, n_in: int, n_out: int, nnz: int, b_in: int = 4, b_out: int = 4,
+                b_val: int = 4) -> int:
+    """Algorithmic bytes of one apply: every input value read once, every
+    output written once, the CSR (int32 column + value per entry, int64 row
+    pointers) read once."""
+    return stack * (n_in * b_in + n_out * b_out) + nnz * (4 + b_val) + (n_out + 1) * 8
+
+
+# ---------------------------------------------------------------------------
+# distributed helpers (replicas: no collective on the data path)
+# ---------------------------------------------------------------------------
+
+
+def dist_env():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return world, rank, local
+
+
+def aggregate_seconds(local_seconds: float, world: int, device=None) -> float:
+    """Max of the per-rank timings (every rank must call this)."""
+    if world <= 1:
+        return local_seconds
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([local_seconds], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+# ---------------------------------------------------------------------------
+# clocks
+# ---------------------------------------------------------------------------
+
+
+class ClockSampler:
+    """nvidia-smi sampled every 50 ms while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,utilization.gpu,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}", "--format=csv,noheader,nounits",
+                 "-lms", "50"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self._t = threading.Thread(target=self._read, daemon=True)
+            self._t.start()
+            time.sleep(0.3)
+        except (OSError, ValueError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            time.sleep(0.1)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        return False
+
+    def summary(self) -> dict:
+        rows = []
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) != 9:
+                continue
+            try:
+                rows.append((float(parts[0]), float(parts[1]), float(parts[2]), float(parts[3]), parts[4:]))
+            except ValueError:
+                continue
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+        load = [r for r in rows if r[3] >= 50] or rows
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        reasons = sorted({names[k] for r in load for k in range(4) if r[4][k + 1].lower() == "active"})
+        return {"sm_mhz": statistics.median(r[0] for r in load), "sm_max_mhz": max(r[1] for r in rows),
+                "reasons": reasons, "samples": len(load), "power_w_max": max(r[2] for r in rows)}
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return float(json.load(f)["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return PEAK_FALLBACK_GBS, "fallback"
+
+
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch recorded from an ncu capture in profiles/."""
+    path = os.path.join(ROOT, "profiles", "traffic.json")
+    try:
+        with open(path) as f:
+            return json.load(f).get(kernel)
+    except (OSError, ValueError):
+        return None
+
+
+def time_launches(fn, steps: int, warmup: int, stream, torch):
+    """Run fn() warmup + steps times; per-launch CUDA-event durations of the
+    timed launches (seconds) and the wall of the whole timed region."""
+    for _ in range(warmup):
+        fn()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    start = torch.cuda.Event(enable_timing=True)
+    end = torch.cuda.Event(enable_timing=True)
+    start.record(stream)
+    for a, b in ev:
+        a.record(stream)
+        fn()
+        b.record(stream)
+    end.record(stream)
+    torch.cuda.synchronize()
+    per = [a.elapsed_time(b) / 1e3 for a, b in ev]
+    return per, start.elapsed_time(end) / 1e3
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import oracle
+    import regridding_gb300 as rg
+    from regridding_gb300 import _device, _lib, workloads
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.current_stream()
+    s_ptr = ctypes.c_void_p(stream.cuda_stream)
+
+    gi, go = workloads.cfg2_grids(N_IN, N_OUT)
+    gop = workloads.perturb(go)
+    n_in_cells = (N_IN - 1) ** 2
+    n_out_cells = (N_OUT - 1) ** 2
+    d_gi = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in gi)
+    d_go = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in gop)
+
+    # --- weight build (each call synchronises to size its buffers)
+    build_ms = []
+    dw = None
+    for _ in range(3):
+        if dw is not None:
+            dw.free()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        dw = rg.build_conservative_2d(d_gi, d_go)
+        torch.cuda.synchronize()
+        build_ms.append((time.perf_counter() - t0) * 1e3)
+    nnz = dw.nnz
+
+    # --- 2D find_indices of the output vertices in the input grid
+    px, py = d_go[0].reshape(-1), d_go[1].reshape(-1)
+    fi_ms = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        oi, oj = rg.locate_2d(d_gi, px, py, method="brute")
+        torch.cuda.synchronize()
+        fi_ms.append((time.perf_counter() - t0) * 1e3)
+    n_outside = int((oi == np.iinfo(np.int64).max).sum().item())
+
+    # --- apply, float32 accumulate (headline)
+    values = workloads.cfg2_values_torch(STACK, N_IN - 1, seed=rank)
+    out32 = torch.empty((STACK, n_out_cells), dtype=torch.float32, device="cuda")
+    out64 = torch.empty((STACK, n_out_cells), dtype=torch.float64, device="cuda")
+    lib = _lib.load()
+    h = dw.handle
+
+    def apply_fast():
+        st = lib.rg_apply(h, ctypes.c_void_p(values.data_ptr()), _lib.RG_F32, ctypes.c_void_p(out32.data_ptr()),
+                          _lib.RG_F32, STACK, _lib.RG_ACC_FAST, s_ptr)
+        if st:
+            _lib.check(st, "rg_apply")
+
+    def apply_exact():
+        st = lib.rg_apply(h, ctypes.c_void_p(values.data_ptr()), _lib.RG_F32, ctypes.c_void_p(out64.data_ptr()),
+                          _lib.RG_F64, STACK, _lib.RG_ACC_EXACT, s_ptr)
+        if st:
+            _lib.check(st, "rg_apply")
+
+    bytes_step = apply_bytes(STACK, n_in_cells, n_out_cells, nnz)
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        per, wall = time_launches(apply_fast, args.steps, args.warmup, stream, torch)
+    barrier(world)
+    wall_max = aggregate_seconds(wall, world, device="cuda")
+    value = world * bytes_step * args.steps / wall_max / 1e9
+    kernel_s = statistics.mean(per)
+
+    per64, wall64 = time_launches(apply_exact, max(5, args.steps // 4), 2, stream, torch)
+    bytes64 = apply_bytes(STACK, n_in_cells, n_out_cells, nnz, b_out=8, b_val=8)
+
+    # --- end to end through the C ABI from page-locked host buffers
+    h_in = torch.empty((STACK, n_in_cells), dtype=torch.float32, pin_memory=True)
+    h_in.copy_(values)
+    h_out = torch.empty((STACK, n_out_cells), dtype=torch.float32, pin_memory=True)
+    torch.cuda.synchronize()
+
+    def apply_host():
+        st = lib.rg_apply_host(h, ctypes.c_void_p(h_in.data_ptr()), _lib.RG_F32, ctypes.c_void_p(h_out.data_ptr()),
+                               _lib.RG_F32, STACK, _lib.RG_ACC_FAST, 0, s_ptr)
+        if st:
+            _lib.check(st, "rg_apply_host")
+
+    e2e_steps = max(3, min(args.steps, 20))
+    per_e2e, wall_e2e = time_launches(apply_host, e2e_steps, 2, stream, torch)
+    e2e_value = world * bytes_step * e2e_steps / aggregate_seconds(wall_e2e, world, device="cuda") / 1e9
+
+    # parity spot check of the headline output against the exact float64 result
+    apply_exact()
+    torch.cuda.synchronize()
+    rel = float(((out32.double() - out64).abs() / out64.abs().clamp_min(1e-30)).max().item())
+
+    # --- CPU baseline: the oracle (C restatement of the upstream loops, all cores)
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        ii, oo, vv = dw.export_numpy()
+        host_vals = h_in.numpy()
+        sample = STACK
+        ts = []
+        for _ in range(2):
+            t0 = time.perf_counter()
+            oracle.apply(ii, oo, vv, host_vals[:sample], n_out_cells)
+            ts.append(time.perf_counter() - t0)
+        t_cpu = min(ts)
+        cpu = {"value": round(apply_bytes(sample, n_in_cells, n_out_cells, nnz) / t_cpu / 1e9, 3), "unit": "GB/s",
+               "cores": os.cpu_count(), "kind": "port",
+               "sample": f"full {sample}-slice apply (float64 output as upstream), best of 2, "
+                         f"{t_cpu * 1e3:.1f} ms"}
+
+    peak, peak_kind = measured_peak()
+    achieved = bytes_step / kernel_s / 1e9
+    traffic = profiled_traffic("apply_kernel_f32")
+    line = {
+        "metric": METRIC,
+        "headline": "apply HBM GB/s, 2048^2 -> 1536^2 conservative weights, 64-deep float32 stack",
+        "value": round(value, 2),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(wall_max / args.steps * 1e3, 4),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32",
+        "data": "synthetic (seeded grids and log-normal stack generated on the device)",
+        "config": {"workload": "2048^2 -> 1536^2 conservative apply, stack 64 float32 (quadratic-mapped input "
+                               "grid, rectilinear output on [-1.05, 1.05]^2)",
+                   "stack": STACK, "input_cells": n_in_cells, "output_cells": n_out_cells, "nnz": nnz,
+                   "bytes_per_step": bytes_step, "l2": "inputs (1.07 GB) exceed L2 (129 MB); no flush",
+                   "parallelism": f"replicas x{world}"},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind},
+        "cpu_baseline": cpu,
+        "e2e": {"value": round(e2e_value, 2), "unit": "GB/s",
+                "h2d_bytes_per_step": STACK * n_in_cells * 4, "d2h_bytes_per_step": STACK * n_out_cells * 4,
+                "ms_per_step": round(wall_e2e / e2e_steps * 1e3, 3), "path": "rg_apply_host, pinned host buffers"},
+        "gpu_launches": args.steps,
+        "clocks": clocks.summary(),
+        "apply_f64_exact": {"GB_per_s": round(bytes64 / statistics.mean(per64) / 1e9, 1),
+                            "ms": round(statistics.mean(per64) * 1e3, 4),
+                            "note": "bit-identical to the upstream float64 apply"},
+        "apply_f32_max_rel_err_vs_f64": rel,
+        "build": {"cells_per_s": round((n_in_cells + n_out_cells) / (min(build_ms) / 1e3), 0),
+                  "ms": [round(v, 2) for v in build_ms], "nnz": nnz},
+        "find_indices_2d": {"points_per_s": round(px.numel() / (min(fi_ms) / 1e3), 0),
+                            "ms": [round(v, 3) for v in fi_ms], "points": int(px.numel()),
+                            "outside": n_outside},
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# reference arm: the upstream algorithm on the host cores (C restatement)
+# ---------------------------------------------------------------------------
+
+
+def run_reference(args, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    from regridding_gb300 import workloads
+
+    gi, go = workloads.cfg2_grids(N_IN, N_OUT)
+    gop = workloads.perturb(go)
+    n_in_cells = (N_IN - 1) ** 2
+    n_out_cells = (N_OUT - 1) ** 2
+    t0 = time.perf_counter()
+    raw = oracle.sweep_2d(gi, gop)
+    t1 = time.perf_counter()
+    ii, oo, vv = oracle.coalesce(*raw)
+    t2 = time.perf_counter()
+    del raw
+    nnz = vv.size
+    rng = np.random.default_rng(0)
+    values = rng.lognormal(3, 1, (STACK, n_in_cells)).astype(np.float32)
+    bytes_step = apply_bytes(STACK, n_in_cells, n_out_cells, nnz)
+    for _ in range(args.warmup):
+        oracle.apply(ii, oo, vv, values, n_out_cells)
+    ts = []
+    for _ in range(args.steps):
+        s = time.perf_counter()
+        oracle.apply(ii, oo, vv, values, n_out_cells)
+        ts.append(time.perf_counter() - s)
+    total = sum(ts)
+    value = bytes_step * args.steps / total / 1e9
+    cores = os.cpu_count()
+    line = {
+        "metric": METRIC,
+        "impl": "reference",
+        "headline": "apply HBM GB/s, 2048^2 -> 1536^2 conservative weights, 64-deep float32 stack",
+        "value": round(value, 3),
+        "unit": "GB/s",
+        "n_gpus": world,
+        "steps": args.steps,
+        "warmup": args.warmup,
+        "ms_per_step": round(total / args.steps * 1e3, 3),
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f64",
+        "data": "synthetic (seeded grids, numpy log-normal stack)",
+        "config": {"workload": "2048^2 -> 1536^2 conservative apply, stack 64 float32", "stack": STACK,
+                   "input_cells": n_in_cells, "output_cells": n_out_cells, "nnz": nnz,
+                   "bytes_per_step": bytes_step, "parallelism": f"{cores} host threads"},
+        "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
+                         "sample": "full 64-slice apply per step (C restatement of the upstream loops, "
+                                   "OpenMP over the stack, float64 output as upstream)"},
+        "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "build": {"cells_per_s": round((n_in_cells + n_out_cells) / (t2 - t0), 0),
+                  "sweep_s": round(t1 - t0, 2), "coalesce_s": round(t2 - t1, 2), "nnz": nnz},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main(argv=None):
+    p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=200)
+    p.add_argument("--warmup", type=int, default=10)
+    p.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = p.parse_args(argv)
+    if args.warmup < 3:
+        args.warmup = 3
+    world, rank, local = dist_env()
+    if args.impl == "reference":
+        # the CPU reference runs on rank 0 only; other ranks exit at once
+        run_reference(args, world, rank)
+        return
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group(backend="nccl")
+    try:
+        run_ours(args, world, rank, local)
+    finally:
+        if world > 1:
+            import torch.distributed as dist
+
+            dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

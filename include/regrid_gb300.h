@@ -116,6 +116,18 @@ int rg_weights_free(rg_weights w, rg_stream_t stream);
 int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dtype_out,
              int64_t stack, int acc, rg_stream_t stream);
 
+/* rg_apply with the stack in HOST memory: h_vin (stack, n_in) and h_vout
+ * (stack, n_out).  The stack is processed in chunks of `chunk` slices (0 =
+ * automatic, about 128 MB of input per chunk) that are copied in, applied
+ * and copied out on separate streams so copies in both directions overlap
+ * the kernels.  This is the entry point for callers that hold their arrays
+ * on the host, as the upstream regrid_from_weights
+ * (regridding/_regrid/_regrid_from_weights.py:12-162) does.  Page-locked
+ * host buffers give full link bandwidth.  Asynchronous: h_vout is complete
+ * once `stream` has been synchronised. */
+int rg_apply_host(rg_weights w, const void* h_vin, int dtype_in, void* h_vout, int dtype_out,
+                  int64_t stack, int acc, int64_t chunk, rg_stream_t stream);
+
 /* The same with the transposed matrix (rows = input cells):
  * values_input[d, i] = sum_o w[o, i] * values_output[d, o].  This is the
  * apply of transpose_weights(),

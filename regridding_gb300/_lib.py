@@ -41,6 +41,7 @@ SIGNATURES = {
     "rg_weights_free": [_P, _P],
     "rg_apply": [_P, _P, _C, _P, _C, _I, _C, _P],
     "rg_apply_transpose": [_P, _P, _C, _P, _C, _I, _C, _P],
+    "rg_apply_host": [_P, _P, _C, _P, _C, _I, _C, _I, _P],
     "rg_cell_area_2d": [_P, _P, _I, _I, _P, _P],
     "rg_cell_length_1d": [_P, _I, _I, _P, _P],
     "rg_locate_2d": [_P, _P, _I, _I, _P, _P, _I, _C, _P, _P, _P],

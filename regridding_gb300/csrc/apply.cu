@@ -176,3 +176,90 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
 }
 
 }  // namespace rg
+
+// ---------------------------------------------------------------------------
+// apply with the stack in host memory: the stack is cut into chunks that are
+// copied in, applied and copied out on three streams, so the two copy
+// directions and the kernels overlap (double-buffered staging in HBM).
+// ---------------------------------------------------------------------------
+namespace rg {
+
+int apply_host(rg_weights_s* W, const void* h_vin, int dtype_in, void* h_vout, int dtype_out,
+               int64_t stack, int acc, int64_t chunk, cudaStream_t s) {
+    RG_CHECK(dtype_in == RG_F32 || dtype_in == RG_F64, RG_ERR_ARG, "apply_host: bad input dtype");
+    RG_CHECK(dtype_out == RG_F32 || dtype_out == RG_F64, RG_ERR_ARG, "apply_host: bad output dtype");
+    if (stack <= 0) return RG_OK;
+    const size_t bin = (dtype_in == RG_F32 ? 4 : 8) * (size_t)W->n_in;
+    const size_t bout = (dtype_out == RG_F32 ? 4 : 8) * (size_t)W->n_out;
+    if (chunk <= 0) {
+        // about 128 MB of input per chunk, at least one slice
+        chunk = (int64_t)((128u << 20) / (bin ? bin : 1));
+        if (chunk < 1) chunk = 1;
+    }
+    if (chunk > stack) chunk = stack;
+    const int64_t nchunks = (stack + chunk - 1) / chunk;
+
+    cudaStream_t sin = nullptr, sout = nullptr;
+    cudaEvent_t ev[2 * 3] = {};
+    char* dbuf[4] = {};
+    int st = RG_OK;
+    do {
+        if (cudaStreamCreateWithFlags(&sin, cudaStreamNonBlocking) != cudaSuccess ||
+            cudaStreamCreateWithFlags(&sout, cudaStreamNonBlocking) != cudaSuccess) {
+            cudaGetLastError();
+            set_error("apply_host: stream creation failed");
+            st = RG_ERR_CUDA;
+            break;
+        }
+        for (int k = 0; k < 6; k++)
+            if (cudaEventCreateWithFlags(&ev[k], cudaEventDisableTiming) != cudaSuccess) {
+                cudaGetLastError();
+                set_error("apply_host: event creation failed");
+                st = RG_ERR_CUDA;
+            }
+        if (st) break;
+        for (int b = 0; b < 2; b++) {
+            if ((st = dalloc(&dbuf[b], bin * chunk, s))) break;
+            if ((st = dalloc(&dbuf[2 + b], bout * chunk, s))) break;
+        }
+        if (st) break;
+        // ev[0..1]: input buffer b consumed by the kernel; ev[2..3]: output
+        // buffer b copied out; ev[4]: input copy of the current chunk landed;
+        // ev[5]: kernel of the current chunk done
+        cudaEventRecord(ev[0], s);
+        cudaEventRecord(ev[1], s);
+        cudaEventRecord(ev[2], s);
+        cudaEventRecord(ev[3], s);
+        for (int64_t c = 0; c < nchunks && st == RG_OK; c++) {
+            int b = (int)(c & 1);
+            int64_t d0 = c * chunk, nd = stack - d0 < chunk ? stack - d0 : chunk;
+            cudaStreamWaitEvent(sin, ev[b], 0);
+            cudaMemcpyAsync(dbuf[b], (const char*)h_vin + d0 * bin, bin * nd, cudaMemcpyHostToDevice, sin);
+            cudaEventRecord(ev[4], sin);
+            cudaStreamWaitEvent(s, ev[4], 0);
+            cudaStreamWaitEvent(s, ev[2 + b], 0);
+            st = apply_weights(W, false, dbuf[b], dtype_in, dbuf[2 + b], dtype_out, nd, acc, s);
+            cudaEventRecord(ev[b], s);
+            cudaEventRecord(ev[5], s);
+            cudaStreamWaitEvent(sout, ev[5], 0);
+            cudaMemcpyAsync((char*)h_vout + d0 * bout, dbuf[2 + b], bout * nd, cudaMemcpyDeviceToHost, sout);
+            cudaEventRecord(ev[2 + b], sout);
+        }
+        // the caller's stream completes after the last copy out
+        cudaStreamWaitEvent(s, ev[2], 0);
+        cudaStreamWaitEvent(s, ev[3], 0);
+        cudaError_t e = cudaGetLastError();
+        if (st == RG_OK && e != cudaSuccess) {
+            set_error("apply_host: %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+        }
+    } while (0);
+    for (int b = 0; b < 4; b++) dfree(dbuf[b], s);
+    for (int k = 0; k < 6; k++)
+        if (ev[k]) cudaEventDestroy(ev[k]);
+    if (sin) cudaStreamDestroy(sin);
+    if (sout) cudaStreamDestroy(sout);
+    return st;
+}
+
+}  // namespace rg

@@ -26,6 +26,7 @@ int locate_2d_exact(const double*, const double*, int64_t, int64_t, const double
 int locate_2d_walk(const double*, const double*, int64_t, int64_t, const double*, const double*, int64_t,
                    int64_t*, int64_t*, cudaStream_t);
 int apply_weights(rg_weights_s*, bool, const void*, int, void*, int, int64_t, int, cudaStream_t);
+int apply_host(rg_weights_s*, const void*, int, void*, int, int64_t, int, int64_t, cudaStream_t);
 int find_indices_1d(const double*, int64_t, int64_t, const double*, int64_t, int64_t, int64_t, int, int64_t,
                     int64_t*, cudaStream_t);
 int multilinear_1d(const double*, int64_t, int64_t, const double*, const double*, int64_t, int64_t, int64_t,
@@ -320,6 +321,12 @@ int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dt
              int acc, rg_stream_t stream) {
     RG_CHECK(w, RG_ERR_ARG, "rg_apply: NULL handle");
     return apply_weights(w, false, d_vin, dtype_in, d_vout, dtype_out, stack, acc, (cudaStream_t)stream);
+}
+
+int rg_apply_host(rg_weights w, const void* h_vin, int dtype_in, void* h_vout, int dtype_out, int64_t stack,
+                  int acc, int64_t chunk, rg_stream_t stream) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_apply_host: NULL handle");
+    return apply_host(w, h_vin, dtype_in, h_vout, dtype_out, stack, acc, chunk, (cudaStream_t)stream);
 }
 
 int rg_apply_transpose(rg_weights w, const void* d_vout, int dtype_out, void* d_vin, int dtype_in,

@@ -1,0 +1,83 @@
+"""Seeded synthetic grids and value stacks for the benchmark configurations.
+
+The upstream publishes no datasets for its benchmarks; these generators make
+grids with the stated shapes and distortions from fixed numpy seeds, so every
+run (and the CPU baseline) sees identical inputs.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+SEED_GEOMETRY = 2
+"""Seed of the cfg2 rotation angle and quadratic-map coefficients."""
+
+
+def distorted_grid(n: int, angle: float, amp: float, lo: float = -1.0, hi: float = 1.0):
+    """``n x n`` vertices on ``[lo, hi]^2`` rotated by ``angle``, then
+    ``x += amp sin(pi y)`` followed by ``y += amp sin(pi x)`` (the second
+    uses the updated x).  This is the 65^2 (0.1 rad, 0.02) small-grid
+    workload and the sinusoidal family of the batched configuration."""
+    a = np.linspace(lo, hi, n)
+    x, y = np.meshgrid(a, a, indexing="ij")
+    xr = x * np.cos(angle) - y * np.sin(angle)
+    yr = x * np.sin(angle) + y * np.cos(angle)
+    xr = xr + amp * np.sin(np.pi * yr)
+    yr = yr + amp * np.sin(np.pi * xr)
+    return xr, yr
+
+
+def rect_grid(n: int, lo: float, hi: float, m: int | None = None):
+    """Rectilinear ``n x m`` vertex grid on ``[lo, hi]^2`` (``indexing="ij"``)."""
+    a = np.linspace(lo, hi, n)
+    b = np.linspace(lo, hi, n if m is None else m)
+    return tuple(np.meshgrid(a, b, indexing="ij"))
+
+
+def quadratic_grid(n: int, seed: int = SEED_GEOMETRY):
+    """``n x n`` vertices on ``[-1, 1]^2`` rotated by ``uniform(0, 0.5)`` rad
+    and distorted by a quadratic polynomial map ``x' = x + sum_k c_k m_k(x, y)``
+    over the monomials (1, x, y, x^2, xy, y^2) with ``c_k ~ N(0, 0.01)``
+    drawn independently for each coordinate (the 2048^2 workload)."""
+    rng = np.random.default_rng(seed)
+    a = np.linspace(-1, 1, n)
+    x, y = np.meshgrid(a, a, indexing="ij")
+    angle = rng.uniform(0, 0.5)
+    xr = x * np.cos(angle) - y * np.sin(angle)
+    yr = x * np.sin(angle) + y * np.cos(angle)
+    cx = rng.normal(0, 0.01, 6)
+    cy = rng.normal(0, 0.01, 6)
+    mono = np.stack([np.ones_like(xr), xr, yr, xr * xr, xr * yr, yr * yr])
+    return xr + np.tensordot(cx, mono, 1), yr + np.tensordot(cy, mono, 1)
+
+
+def perturb(grid, seed: int = 42):
+    """The default output-grid perturbation of ``weights(method="conservative")``:
+    ``default_rng(seed).normal(c, ptp(c) * 1e-9)`` per coordinate, x then y."""
+    rng = np.random.default_rng(seed)
+    return tuple(rng.normal(c, np.ptp(c) * 1e-9) for c in grid)
+
+
+def cfg1():
+    """65^2 -> 49^2 conservative regrid of 8 Poisson(100) float64 arrays."""
+    gi = distorted_grid(65, 0.1, 0.02)
+    go = rect_grid(49, -1.1, 1.1)
+    values = np.random.default_rng(42).poisson(100, (8, 64, 64)).astype(np.float64)
+    return gi, go, values
+
+
+def cfg2_grids(n_in: int = 2049, n_out: int = 1537):
+    """2048^2 -> 1536^2 grids: quadratic-mapped input, rectilinear output on
+    [-1.05, 1.05]^2."""
+    return quadratic_grid(n_in), rect_grid(n_out, -1.05, 1.05)
+
+
+def cfg2_values_torch(stack: int = 64, n: int = 2048, seed: int = 0, device="cuda"):
+    """float32 log-normal(3, 1) stack generated on the device (seeded)."""
+    import torch
+
+    g = torch.Generator(device=device)
+    g.manual_seed(seed)
+    v = torch.empty((stack, n * n), dtype=torch.float32, device=device)
+    v.normal_(mean=3.0, std=1.0, generator=g)
+    return v.exp_()

@@ -400,3 +400,35 @@ def test_degenerate_grids_report_walk_error(rg):
     rng = np.random.default_rng(42)
     gop = tuple(rng.normal(a, np.ptp(a) * 1e-9) for a in go)
     assert rg.build_conservative_2d(gi, gop).nnz > 0
+
+
+def test_apply_from_host_buffers(rg):
+    """rg_apply_host (chunked, three streams) equals the device apply."""
+    import ctypes
+
+    import torch
+    from regridding_gb300 import _lib
+
+    c = CURVI.case("curvi129")
+    w = rg.weights(c.tuple("ci"), c.tuple("co"), method="conservative")
+    (ii, oo, vv), = w[0].reshape(-1)
+    dw = rg.DeviceWeights.from_coo(ii, oo, vv, 128 * 128, 96 * 96, (96, 96))
+    rng = np.random.default_rng(1)
+    vals = rng.lognormal(3, 1, (37, 128 * 128)).astype(np.float32)
+    ref = dw.apply(torch.from_numpy(vals).cuda(), accumulate="fast").cpu().numpy()
+    h_in = torch.from_numpy(vals).pin_memory()
+    for chunk in (0, 1, 5, 37, 100):
+        h_out = torch.zeros((37, 96 * 96), dtype=torch.float32).pin_memory()
+        s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        _lib.call("rg_apply_host", dw.handle, ctypes.c_void_p(h_in.data_ptr()), _lib.RG_F32,
+                  ctypes.c_void_p(h_out.data_ptr()), _lib.RG_F32, 37, _lib.RG_ACC_FAST, chunk, s)
+        torch.cuda.synchronize()
+        assert_same(h_out.numpy(), ref)
+    # exact float64 output from float64 host input, pageable memory
+    v64 = vals.astype(np.float64)
+    out64 = np.zeros((37, 96 * 96))
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.call("rg_apply_host", dw.handle, ctypes.c_void_p(v64.ctypes.data), _lib.RG_F64,
+              ctypes.c_void_p(out64.ctypes.data), _lib.RG_F64, 37, _lib.RG_ACC_EXACT, 8, s)
+    torch.cuda.synchronize()
+    assert_same(out64, oracle.apply(ii, oo, vv, v64, 96 * 96))

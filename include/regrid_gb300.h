@@ -159,6 +159,28 @@ int rg_locate_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, c
                  const double* d_py, int64_t npts, int method, int64_t* d_i, int64_t* d_j,
                  rg_stream_t stream);
 
+/* Largest point count of one rg_locate_2d_noalloc call. */
+#define RG_LOCATE_NOALLOC_MAX_POINTS 1048576
+
+/* rg_locate_2d with method 2 (grid walk) that allocates no device memory.
+ * This entry point has no counterpart in the upstream package.  It serves
+ * callers that cannot allocate at call time: processes whose device memory is
+ * owned by another allocator or a fixed budget, and latency-critical loops
+ * that must not meet an allocation's implicit synchronisation or an
+ * out-of-memory failure mid-stream.  The scratch it needs (the points the walk
+ * hands to the exhaustive fallback) is a static device array of
+ * 8 * (32 + RG_LOCATE_NOALLOC_MAX_POINTS) bytes (about 8 MiB) that every GPU
+ * which loads the library holds until the process exits.  The first call on
+ * each device looks up that array's device address (with the device
+ * current); make that first call before capturing the stream into a graph.
+ * At most RG_LOCATE_NOALLOC_MAX_POINTS points per call (RG_ERR_ARG beyond).
+ * Every call on a device shares the one array, so calls that overlap on the
+ * GPU (different streams, or host threads) race and must be serialised.
+ * Results equal rg_locate_2d with method 2. */
+int rg_locate_2d_noalloc(const double* d_x, const double* d_y, int64_t nx, int64_t ny,
+                         const double* d_px, const double* d_py, int64_t npts, int64_t* d_i,
+                         int64_t* d_j, rg_stream_t stream);
+
 /* 1D find_indices on a batch of nd rows.  method 0 = brute
  * (_find_indices_brute_1d, regridding/_find_indices/_find_indices_brute.py:24-51),
  * method 1 = searchsorted (_find_indices_searchsorted_1d,

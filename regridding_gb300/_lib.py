@@ -45,6 +45,7 @@ SIGNATURES = {
     "rg_cell_area_2d": [_P, _P, _I, _I, _P, _P],
     "rg_cell_length_1d": [_P, _I, _I, _P, _P],
     "rg_locate_2d": [_P, _P, _I, _I, _P, _P, _I, _C, _P, _P, _P],
+    "rg_locate_2d_noalloc": [_P, _P, _I, _I, _P, _P, _I, _P, _P, _P],
     "rg_find_indices_1d": [_P, _I, _I, _P, _I, _I, _I, _C, _I, _P, _P],
     "rg_multilinear_1d": [_P, _I, _I, _P, _P, _I, _I, _I, _P, _I, _C, _P, _P, _P, ctypes.POINTER(_I), _P],
     "rg_conservative_1d": [_P, _I, _I, _P, _I, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P],

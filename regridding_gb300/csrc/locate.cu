@@ -12,6 +12,7 @@
 // warp each: a lane-parallel winding test against the whole grid boundary
 // decides "outside", otherwise a lane-parallel exhaustive scan answers.
 #include <cmath>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -242,3 +243,76 @@ int locate_2d_walk(const double* x, const double* y, int64_t nx, int64_t ny, con
 }
 
 }  // namespace rg
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of the walk locator.
+//
+// Some callers cannot allocate device memory at call time: a host process
+// whose device memory is entirely owned by another allocator (a framework
+// pool or a fixed serving budget), or a latency-critical loop that must not
+// risk the implicit synchronisation or the out-of-memory failure of an
+// allocation in the middle of its work.  For them, the only scratch the
+// walk locator needs -- the list of points the walk hands to the warp
+// fallback, and its counter -- lives in the file-scope array below, which
+// the CUDA runtime places in device memory once per device when the library
+// is loaded there and keeps until the process exits.
+// ---------------------------------------------------------------------------
+namespace rg {
+namespace {
+
+constexpr int64_t kNoallocMaxPoints = RG_LOCATE_NOALLOC_MAX_POINTS;
+
+// word 0: number of points left to the fallback; words 32..: their indices
+static __device__ __align__(256) unsigned long long g_locate_scratch[32 + kNoallocMaxPoints];
+
+std::mutex g_scratch_mutex;
+void* g_scratch_address[256] = {};  // per device ordinal, filled on first use
+
+// Device address of g_locate_scratch on the current device.  In host code the
+// array's name only stands in for the symbol, so the address is looked up
+// once per device, with that device current.
+int scratch_address(void** out) {
+    int dev = 0;
+    RG_CUDA(cudaGetDevice(&dev));
+    RG_CHECK(dev >= 0 && dev < 256, RG_ERR_UNSUPPORTED, "device ordinal %d out of range", dev);
+    std::lock_guard<std::mutex> lock(g_scratch_mutex);
+    if (g_scratch_address[dev] == nullptr) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_locate_scratch);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            set_error("rg_locate_2d_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+            return RG_ERR_CUDA;
+        }
+        g_scratch_address[dev] = p;
+    }
+    *out = g_scratch_address[dev];
+    return RG_OK;
+}
+
+}  // namespace
+}  // namespace rg
+
+extern "C" int rg_locate_2d_noalloc(const double* d_x, const double* d_y, int64_t nx, int64_t ny,
+                                    const double* d_px, const double* d_py, int64_t npts, int64_t* d_i,
+                                    int64_t* d_j, rg_stream_t stream) {
+    using namespace rg;
+    RG_CHECK(nx >= 2 && ny >= 2, RG_ERR_ARG, "rg_locate_2d_noalloc: need at least 2x2 vertices");
+    RG_CHECK(npts >= 0 && npts <= kNoallocMaxPoints, RG_ERR_ARG,
+             "rg_locate_2d_noalloc: %lld points requested, at most %lld per call (split the call, or use "
+             "rg_locate_2d, which allocates its scratch)",
+             (long long)npts, (long long)kNoallocMaxPoints);
+    if (npts == 0) return RG_OK;
+    void* base = nullptr;
+    RG_TRY(scratch_address(&base));
+    cudaStream_t s = (cudaStream_t)stream;
+    unsigned long long* nfail = (unsigned long long*)base;
+    int64_t* fails = (int64_t*)((unsigned long long*)base + 32);
+    // the array keeps the previous call's contents: the counter starts at zero
+    RG_CUDA(cudaMemsetAsync(nfail, 0, sizeof(unsigned long long), s));
+    G2 g{d_x, d_y, nx, ny};
+    locate_walk_kernel<<<grid_for(npts, 128), 128, 0, s>>>(g, d_px, d_py, npts, d_i, d_j, fails, nfail);
+    locate_fallback_kernel<<<1024, 128, 0, s>>>(g, d_px, d_py, fails, nfail, d_i, d_j);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}

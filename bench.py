@@ -191,6 +191,27 @@ def time_launches(fn, steps: int, warmup: int, stream, torch):
     return per, start.elapsed_time(end) / 1e3
 
 
+def run_quick(args, local):
+    """Build + fast apply only, at a chosen size: the command profiled by ncu."""
+    import torch
+
+    import regridding_gb300 as rg
+    from regridding_gb300 import workloads
+
+    torch.cuda.set_device(local)
+    gi, go = workloads.cfg2_grids(args.n_in, args.n_out)
+    gop = workloads.perturb(go)
+    dw = rg.build_conservative_2d(gi, gop)
+    values = workloads.cfg2_values_torch(args.stack, args.n_in - 1)
+    out = torch.empty((args.stack, (args.n_out - 1) ** 2), dtype=torch.float32, device="cuda")
+    per, wall = time_launches(lambda: dw.apply(values, out=out, accumulate="fast"), args.steps, args.warmup,
+                              torch.cuda.current_stream(), torch)
+    b = apply_bytes(args.stack, (args.n_in - 1) ** 2, (args.n_out - 1) ** 2, dw.nnz)
+    print(json.dumps({"quick": True, "n_in": args.n_in, "n_out": args.n_out, "stack": args.stack, "nnz": dw.nnz,
+                      "bytes_per_launch": b, "kernel_ms": statistics.mean(per) * 1e3,
+                      "GB_per_s": b / statistics.mean(per) / 1e9}), flush=True)
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -417,6 +438,11 @@ def main(argv=None):
     p.add_argument("--warmup", type=int, default=10)
     p.add_argument("--impl", choices=("ours", "reference"), default="ours")
     p.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    p.add_argument("--quick", action="store_true",
+                   help="build + fast apply only at --n-in/--n-out/--stack (for profiling)")
+    p.add_argument("--n-in", type=int, default=N_IN)
+    p.add_argument("--n-out", type=int, default=N_OUT)
+    p.add_argument("--stack", type=int, default=STACK)
     args = p.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -424,6 +450,9 @@ def main(argv=None):
     if args.impl == "reference":
         # the CPU reference runs on rank 0 only; other ranks exit at once
         run_reference(args, world, rank)
+        return
+    if args.quick:
+        run_quick(args, local)
         return
     if world > 1:
         import torch

@@ -166,8 +166,20 @@ int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, flo
 
 }  // namespace
 
+int apply_tiled(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+
 int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_in, void* vout,
                   int dtype_out, int64_t stack, int acc, cudaStream_t s) {
+    if (!transposed && acc == RG_ACC_FAST && dtype_in == RG_F32 && dtype_out == RG_F32 && stack > 0 &&
+        W->n_out > 0 && W->nnz > 0) {
+        // the bandwidth path: float32 in and out, gather lists staged in shared memory
+        if (W->val32 == nullptr) {
+            RG_TRY(dalloc(&W->val32, (size_t)W->nnz, s));
+            to_f32<<<grid_for(W->nnz, 256) > 8192 ? 8192 : grid_for(W->nnz, 256), 256, 0, s>>>(W->val, W->val32,
+                                                                                              W->nnz);
+        }
+        return apply_tiled(W, (const float*)vin, (float*)vout, stack, s);
+    }
     if (!transposed)
         return apply_csr(W->row_ptr, W->col, W->val, &W->val32, W->nnz, W->n_out, W->n_in, W->out_shape0,
                          W->out_shape1, vin, dtype_in, vout, dtype_out, stack, acc, s);

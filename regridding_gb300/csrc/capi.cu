@@ -173,6 +173,11 @@ void free_weights(rg_weights_s* W, cudaStream_t s) {
     dfree(W->t_col, s);
     dfree(W->t_val, s);
     dfree(W->t_val32, s);
+    for (int g = 0; g < 2; g++) {
+        dfree(W->t_gptr[g], s);
+        dfree(W->t_gidx[g], s);
+        dfree(W->t_slot[g], s);
+    }
     delete W;
 }
 

@@ -123,5 +123,13 @@ struct rg_weights_s {
     float* t_val32 = nullptr;
     // (optional) output grid shape for 2D tiling of the apply
     int64_t out_shape0 = 0, out_shape1 = 0;
+    // warp-tile lists of the float32 fast apply, built on first use; index 0
+    // lists single cells, index 1 lists 32-byte sectors of 8 cells
+    bool tiled_ready[2] = {false, false};
+    int64_t t_tiles = 0;
+    int t_gmax[2] = {0, 0};
+    int64_t* t_gptr[2] = {nullptr, nullptr};   // [tiles + 1]
+    int32_t* t_gidx[2] = {nullptr, nullptr};   // the lists
+    uint16_t* t_slot[2] = {nullptr, nullptr};  // [nnz] staged slot of each entry
     int device = 0;
 };

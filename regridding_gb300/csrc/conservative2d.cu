@@ -28,6 +28,8 @@
 //     numpy's add.reduceat association (first + pairwise rest), giving a CSR
 //     matrix whose values are bit-identical to the upstream coalesced ones.
 #include <cmath>
+#include <cstdlib>
+#include <cstring>
 
 #include "common.cuh"
 
@@ -242,11 +244,14 @@ __global__ void cell_area_kernel(const double* __restrict__ x, const double* __r
     }
 }
 
-__global__ void bbox_kernel(const double* x, const double* y, int64_t n, double* out4) {
-    // out4 = (xmin, ymin, xmax, ymax); single block
+// Bounding box (xmin, ymin, xmax, ymax) of a vertex grid: per-block partial
+// extrema, then one block combines them (min/max are exact in any order).
+__global__ void bbox_partial(const double* __restrict__ x, const double* __restrict__ y, int64_t n,
+                             double* __restrict__ part) {
     __shared__ double s[4][256];
     double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
-    for (int64_t k = threadIdx.x; k < n; k += blockDim.x) {
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
+         k += (int64_t)gridDim.x * blockDim.x) {
         double xv = x[k], yv = y[k];
         a = fmin(a, xv);
         b = fmin(b, yv);
@@ -267,7 +272,22 @@ __global__ void bbox_kernel(const double* x, const double* y, int64_t n, double*
         }
         __syncthreads();
     }
-    if (threadIdx.x < 4) out4[threadIdx.x] = s[threadIdx.x][0];
+    if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = s[threadIdx.x][0];
+}
+
+__global__ void bbox_combine(const double* __restrict__ part, int nparts, double* __restrict__ out4) {
+    if (threadIdx.x != 0) return;
+    double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+    for (int k = 0; k < nparts; k++) {
+        a = fmin(a, part[4 * k]);
+        b = fmin(b, part[4 * k + 1]);
+        c = fmax(c, part[4 * k + 2]);
+        d = fmax(d, part[4 * k + 3]);
+    }
+    out4[0] = a;
+    out4[1] = b;
+    out4[2] = c;
+    out4[3] = d;
 }
 
 // Boundary polygon of grid_boundary (_grids.py:167-215), vertex k.
@@ -474,34 +494,37 @@ __constant__ int c_vtx_j[4] = {0, 0, 1, 1};
 __constant__ int c_nrm_i[4] = {-1, 0, 1, 0};  // cell_normals: _grids.py:143-148
 __constant__ int c_nrm_j[4] = {0, -1, 0, 1};
 
-// One thread per sweep line: the body of the prange loop of _sweep_along_axis
-// (:432-533) with _step_outside_static (:547-698), _step_inside_static
-// (:707-895) and _calc_and_save_weights (:903-976) inlined.  COUNT mode only
-// counts the triples a line emits; WRITE mode stores them from offsets[line].
-template <bool WRITE>
-__global__ void __launch_bounds__(64)
-    walk_kernel(SweepParams P, const Seat* __restrict__ seats, int64_t* __restrict__ counts,
-                const int64_t* __restrict__ offsets, int32_t* __restrict__ raw_in,
-                int32_t* __restrict__ raw_out, double* __restrict__ raw_val, unsigned* flags) {
-    int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (line >= P.total_lines) return;
-    const Family F = P.fam[family_of(P, line)];
-    const Static& S = P.st[F.st];
-    const Grid st = S.g;
-    const int64_t li = line - F.line_base;
-    Seat seat = seats[line];
-    int64_t stx = seat.stx, sty = seat.sty;
-    bool outside = seat.outside;
-    int64_t edge_last = MAXSIZE;
-    int64_t sy_idx = 0;
-    int64_t n_emit = 0;
-    int64_t wpos = WRITE ? offsets[line] : 0;
-    const int64_t wend = WRITE ? offsets[line + 1] : 0;
-    const int64_t max_steps = 64 * (F.len + 4 * (S.ncx + S.ncy) + 16);
-    int64_t steps = 0;
-    double x1 = F.SX(li, 0), y1 = F.SY(li, 0);
+// State of a walk at a sweep vertex.  At every vertex the upstream's
+// entry-edge marker is back at sys.maxsize and the current point is the
+// vertex itself, so (outside, static cell) is the whole state.
+struct WalkState {
+    int64_t stx, sty;
+    int64_t sy;  // index of the sweep vertex the walk is at
+    int outside;
+    int pad;
+};
 
-    while (sy_idx < F.len - 1) {
+// The body of the prange loop of _sweep_along_axis (:432-533) with
+// _step_outside_static (:547-698), _step_inside_static (:707-895) and
+// _calc_and_save_weights (:903-976) inlined, run on line li from vertex
+// st.sy until the walk reaches vertex j_end.  WRITE stores triples at
+// [wpos, wend); past wend it only counts (and flags the overflow).  Returns
+// the number of triples emitted.
+template <bool WRITE>
+__device__ int64_t walk_range(const SweepParams& P, const Family& F, const Static& S, int64_t li, int64_t j_end,
+                              WalkState& state, int64_t wpos, int64_t wend, int32_t* __restrict__ raw_in,
+                              int32_t* __restrict__ raw_out, double* __restrict__ raw_val, unsigned* flags,
+                              int64_t max_steps) {
+    const Grid st = S.g;
+    int64_t stx = state.stx, sty = state.sty;
+    bool outside = state.outside;
+    int64_t edge_last = MAXSIZE;
+    int64_t sy_idx = state.sy;
+    int64_t n_emit = 0;
+    int64_t steps = 0;
+    double x1 = F.SX(li, sy_idx), y1 = F.SY(li, sy_idx);
+
+    while (sy_idx < j_end) {
         if (++steps > max_steps) {
             atomicOr(flags, FLAG_WALK_CAP);
             break;
@@ -604,16 +627,17 @@ __global__ void __launch_bounds__(64)
                 else { ii = stx; ij = sty; oi = a; oj = b; }
                 int64_t in_flat = ii * P.ncy_in + ij;
                 if (WRITE) {
-                    if (wpos >= wend) {  // the count walk disagreed: never write past the line's slots
+                    if (wpos < wend) {
+                        double ain = __ldg(P.area_in + in_flat);
+                        double w = side == 0 ? ddiv(area, ain) : ddiv(-area, ain);
+                        if (P.w_in) w = dmul(w, __ldg(P.w_in + in_flat));
+                        raw_in[wpos] = (int32_t)in_flat;
+                        raw_out[wpos] = (int32_t)(oi * P.ncy_out + oj);
+                        raw_val[wpos] = w;
+                    } else {
+                        // never write past the slots given to this walk
                         atomicOr(flags, FLAG_CAPACITY);
-                        continue;
                     }
-                    double ain = __ldg(P.area_in + in_flat);
-                    double w = side == 0 ? ddiv(area, ain) : ddiv(-area, ain);
-                    if (P.w_in) w = dmul(w, __ldg(P.w_in + in_flat));
-                    raw_in[wpos] = (int32_t)in_flat;
-                    raw_out[wpos] = (int32_t)(oi * P.ncy_out + oj);
-                    raw_val[wpos] = w;
                     wpos++;
                 }
                 n_emit++;
@@ -631,7 +655,219 @@ __global__ void __launch_bounds__(64)
         x1 = x2;
         y1 = y2;
     }
-    if (!WRITE) counts[line] = n_emit;
+    state.stx = stx;
+    state.sty = sty;
+    state.sy = sy_idx;
+    state.outside = outside;
+    return n_emit;
+}
+
+// One thread per sweep line over the whole line.  COUNT mode only counts the
+// triples a line emits; WRITE mode stores them from offsets[line].
+template <bool WRITE>
+__global__ void __launch_bounds__(64)
+    walk_kernel(SweepParams P, const Seat* __restrict__ seats, int64_t* __restrict__ counts,
+                const int64_t* __restrict__ offsets, int32_t* __restrict__ raw_in,
+                int32_t* __restrict__ raw_out, double* __restrict__ raw_val, unsigned* flags) {
+    int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (line >= P.total_lines) return;
+    const Family F = P.fam[family_of(P, line)];
+    const Static& S = P.st[F.st];
+    Seat seat = seats[line];
+    WalkState state{seat.stx, seat.sty, 0, seat.outside, 0};
+    const int64_t max_steps = 64 * (F.len + 4 * (S.ncx + S.ncy) + 16);
+    int64_t n = walk_range<WRITE>(P, F, S, line - F.line_base, F.len - 1, state,
+                                  WRITE ? offsets[line] : 0, WRITE ? offsets[line + 1] : 0, raw_in, raw_out,
+                                  raw_val, flags, max_steps);
+    if (!WRITE) counts[line] = n;
+}
+
+// ---------------------------------------------------------------------------
+// chunked walk: every line is cut into chunks of CH sweep segments that are
+// walked in parallel.  A chunk starts from its vertex located in the static
+// grid; a per-line repair pass then re-walks, in order, every chunk whose
+// start disagrees with the end state of the chunk before it, so the triples
+// are exactly those of one sequential walk per line.
+// ---------------------------------------------------------------------------
+
+struct ChunkPlan {
+    int64_t ch;              // sweep segments per chunk
+    int64_t nc[4];           // chunks per line, per family
+    int64_t chunk_base[5];   // first chunk id of each family (and the total)
+    int64_t cap[4];          // triple slots per chunk, per family
+    int64_t slot_base[4];    // first slot of each family
+};
+
+__device__ __forceinline__ int family_of_chunk(const ChunkPlan& C, int64_t g) {
+    int f = 0;
+#pragma unroll
+    for (int k = 1; k < 4; k++)
+        if (g >= C.chunk_base[k]) f = k;
+    return f;
+}
+
+__device__ __forceinline__ double bilinear_fast(const double* a, int64_t sx, int64_t sy, double x, double y) {
+    int64_t x0 = (int64_t)floor(x), y0 = (int64_t)floor(y);
+    x0 = x0 < 0 ? 0 : (x0 > sx - 2 ? sx - 2 : x0);
+    y0 = y0 < 0 ? 0 : (y0 > sy - 2 ? sy - 2 : y0);
+    double dx = x - x0, dy = y - y0;
+    double a00 = __ldg(a + x0 * sy + y0), a01 = __ldg(a + x0 * sy + y0 + 1);
+    double a10 = __ldg(a + (x0 + 1) * sy + y0), a11 = __ldg(a + (x0 + 1) * sy + y0 + 1);
+    return a00 * (1 - dx) * (1 - dy) + a01 * (1 - dx) * dy + a10 * dx * (1 - dy) + a11 * dx * dy;
+}
+
+// A guess of the walk state at a sweep vertex: the static cell containing
+// it (Newton seed on the bilinear index map, then a walk across the edge the
+// point lies beyond), or "outside".  Wrong guesses are fixed by the repair.
+__device__ WalkState guess_state(const Static& S, double px, double py, int64_t sy) {
+    WalkState w{MAXSIZE, MAXSIZE, sy, 1, 0};
+    if (!((S.blx <= px && px <= S.bux) && (S.bly <= py && py <= S.buy))) return w;
+    const Grid& g = S.g;
+    const int64_t ncx = S.ncx, ncy = S.ncy;
+    double fi = 0.5 * (double)ncx, fj = 0.5 * (double)ncy;
+    for (int it = 0; it < 10; it++) {
+        double xv = bilinear_fast(g.x, g.nx, g.ny, fi, fj), yv = bilinear_fast(g.y, g.nx, g.ny, fi, fj);
+        const double h = 1e-3;
+        double xi = (bilinear_fast(g.x, g.nx, g.ny, fi + h, fj) - xv) / h;
+        double xj = (bilinear_fast(g.x, g.nx, g.ny, fi, fj + h) - xv) / h;
+        double yi = (bilinear_fast(g.y, g.nx, g.ny, fi + h, fj) - yv) / h;
+        double yj = (bilinear_fast(g.y, g.nx, g.ny, fi, fj + h) - yv) / h;
+        double det = xi * yj - xj * yi;
+        if (!(det != 0) || !isfinite(det)) break;
+        double ex = xv - px, ey = yv - py;
+        double di = (yj * ex - xj * ey) / det, dj = (-yi * ex + xi * ey) / det;
+        fi = fmin(fmax(fi - di, 0.0), (double)ncx - 1e-9);
+        fj = fmin(fmax(fj - dj, 0.0), (double)ncy - 1e-9);
+        if (fabs(di) < 1e-3 && fabs(dj) < 1e-3) break;
+    }
+    int64_t ci = (int64_t)floor(fi), cj = (int64_t)floor(fj);
+    ci = ci < 0 ? 0 : (ci >= ncx ? ncx - 1 : ci);
+    cj = cj < 0 ? 0 : (cj >= ncy ? ncy - 1 : cj);
+    for (int step = 0; step < 64; step++) {
+        if (cell_contains(g, ci, cj, px, py)) {
+            w.stx = ci;
+            w.sty = cj;
+            w.outside = 0;
+            return w;
+        }
+        double vx[4] = {g.X(ci, cj), g.X(ci + 1, cj), g.X(ci + 1, cj + 1), g.X(ci, cj + 1)};
+        double vy[4] = {g.Y(ci, cj), g.Y(ci + 1, cj), g.Y(ci + 1, cj + 1), g.Y(ci, cj + 1)};
+        double area2 = (vx[0] - vx[2]) * (vy[1] - vy[3]) - (vx[1] - vx[3]) * (vy[0] - vy[2]);
+        double sgn = area2 >= 0 ? 1.0 : -1.0;
+        int best = -1;
+        double worst = 0;
+#pragma unroll
+        for (int e = 0; e < 4; e++) {
+            int f = (e + 1) & 3;
+            double ex = vx[f] - vx[e], ey = vy[f] - vy[e];
+            double cr = sgn * (ex * (py - vy[e]) - ey * (px - vx[e]));
+            double len = sqrt(ex * ex + ey * ey);
+            double sc = len > 0 ? cr / len : 0;
+            if (sc < worst) {
+                worst = sc;
+                best = e;
+            }
+        }
+        if (best < 0) break;
+        const int di[4] = {0, 1, 0, -1};
+        const int dj[4] = {-1, 0, 1, 0};
+        int64_t ni = ci + di[best], nj = cj + dj[best];
+        if (ni < 0 || nj < 0 || ni >= ncx || nj >= ncy) break;
+        ci = ni;
+        cj = nj;
+    }
+    return w;
+}
+
+__global__ void chunk_seat_kernel(SweepParams P, ChunkPlan C, const Seat* __restrict__ seats,
+                                  WalkState* __restrict__ starts) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= C.chunk_base[4]) return;
+    int f = family_of_chunk(C, g);
+    const Family& F = P.fam[f];
+    int64_t k = g - C.chunk_base[f];
+    int64_t li = k / C.nc[f], c = k - li * C.nc[f];
+    int64_t j0 = c * C.ch;
+    if (c == 0) {
+        Seat s0 = seats[F.line_base + li];
+        starts[g] = WalkState{s0.stx, s0.sty, 0, s0.outside, 0};
+    } else {
+        starts[g] = guess_state(P.st[F.st], F.SX(li, j0), F.SY(li, j0), j0);
+    }
+}
+
+__device__ __forceinline__ int64_t chunk_end(const ChunkPlan& C, const Family& F, int64_t c) {
+    int64_t e = (c + 1) * C.ch;
+    return e < F.len - 1 ? e : F.len - 1;
+}
+
+__global__ void __launch_bounds__(64)
+    chunk_walk_kernel(SweepParams P, ChunkPlan C, const WalkState* __restrict__ starts,
+                      WalkState* __restrict__ ends, int64_t* __restrict__ counts, int32_t* __restrict__ s_in,
+                      int32_t* __restrict__ s_out, double* __restrict__ s_val, unsigned* flags) {
+    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (g >= C.chunk_base[4]) return;
+    int f = family_of_chunk(C, g);
+    const Family F = P.fam[f];
+    const Static& S = P.st[F.st];
+    int64_t k = g - C.chunk_base[f];
+    int64_t li = k / C.nc[f], c = k - li * C.nc[f];
+    WalkState st = starts[g];
+    int64_t base = C.slot_base[f] + k * C.cap[f];
+    const int64_t max_steps = 64 * (C.ch + 4 * (S.ncx + S.ncy) + 16);
+    counts[g] = walk_range<true>(P, F, S, li, chunk_end(C, F, c), st, base, base + C.cap[f], s_in, s_out,
+                                 s_val, flags, max_steps);
+    ends[g] = st;
+}
+
+// One thread per line: walk chunks again, in order, wherever a chunk's start
+// differs from the previous chunk's end.
+__global__ void __launch_bounds__(64)
+    chunk_repair_kernel(SweepParams P, ChunkPlan C, WalkState* __restrict__ starts, WalkState* __restrict__ ends,
+                        int64_t* __restrict__ counts, int32_t* __restrict__ s_in, int32_t* __restrict__ s_out,
+                        double* __restrict__ s_val, unsigned* flags, unsigned long long* __restrict__ n_repaired) {
+    int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (line >= P.total_lines) return;
+    int f = family_of(P, line);
+    const Family F = P.fam[f];
+    const Static& S = P.st[F.st];
+    int64_t li = line - F.line_base;
+    const int64_t max_steps = 64 * (C.ch + 4 * (S.ncx + S.ncy) + 16);
+    int64_t g0 = C.chunk_base[f] + li * C.nc[f];
+    for (int64_t c = 1; c < C.nc[f]; c++) {
+        WalkState prev = ends[g0 + c - 1];
+        WalkState cur = starts[g0 + c];
+        bool same = prev.outside == cur.outside && (prev.outside || (prev.stx == cur.stx && prev.sty == cur.sty));
+        if (same) continue;
+        atomicAdd(n_repaired, 1ull);
+        starts[g0 + c] = prev;
+        WalkState st = prev;
+        int64_t k = li * C.nc[f] + c;
+        int64_t base = C.slot_base[f] + k * C.cap[f];
+        counts[g0 + c] = walk_range<true>(P, F, S, li, chunk_end(C, F, c), st, base, base + C.cap[f], s_in,
+                                          s_out, s_val, flags, max_steps);
+        ends[g0 + c] = st;
+    }
+}
+
+// One warp per chunk: move its triples from its slots to their place in the
+// emission order.
+__global__ void chunk_compact_kernel(ChunkPlan C, const int64_t* __restrict__ counts,
+                                     const int64_t* __restrict__ offsets, const int32_t* __restrict__ s_in,
+                                     const int32_t* __restrict__ s_out, const double* __restrict__ s_val,
+                                     int32_t* __restrict__ raw_in, int32_t* __restrict__ raw_out,
+                                     double* __restrict__ raw_val) {
+    int lane = threadIdx.x & 31;
+    int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (g >= C.chunk_base[4]) return;
+    int f = family_of_chunk(C, g);
+    int64_t base = C.slot_base[f] + (g - C.chunk_base[f]) * C.cap[f];
+    int64_t n = counts[g], dst = offsets[g];
+    for (int64_t q = lane; q < n; q += 32) {
+        raw_in[dst + q] = s_in[base + q];
+        raw_out[dst + q] = s_out[base + q];
+        raw_val[dst + q] = s_val[base + q];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -860,6 +1096,163 @@ int locate_2d_exact(const double* x, const double* y, int64_t nx, int64_t ny, co
     return RG_OK;
 }
 
+namespace {
+
+int check_walk_flags(unsigned fl) {
+    if (fl & (FLAG_WALK_CAP | FLAG_SEAT_OUTSIDE)) {
+        set_error("conservative sweep: %s",
+                  (fl & FLAG_WALK_CAP) ? "a grid line exceeded its step cap (degenerate grids?)"
+                                       : "a grid line starting inside the grid boundary could "
+                                         "not be located in any cell");
+        return RG_ERR_WALK;
+    }
+    return RG_OK;
+}
+
+// One thread per line, count then write (synchronises once).
+int sweep_lines(const SweepParams& P, const Seat* seats, unsigned* flags, int64_t* total_dev, cudaStream_t s,
+                int32_t** raw_in, int32_t** raw_out, double** raw_val, int64_t* nraw_out) {
+    const int64_t base = P.total_lines;
+    int64_t *counts = nullptr, *offsets = nullptr;
+    int st = RG_OK;
+    do {
+        if ((st = dalloc(&counts, (size_t)base + 1, s))) break;
+        if ((st = dalloc(&offsets, (size_t)base + 1, s))) break;
+        walk_kernel<false><<<grid_for(base, 64), 64, 0, s>>>(P, seats, counts, nullptr, nullptr, nullptr, nullptr,
+                                                             flags);
+        cudaMemsetAsync(counts + base, 0, sizeof(int64_t), s);
+        if ((st = exclusive_scan_i64(counts, offsets, base + 1, total_dev, s))) break;
+        int64_t nraw = 0;
+        unsigned fl = 0;
+        cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("conservative sweep (count walk): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        if ((st = check_walk_flags(fl))) break;
+        if (nraw >= (int64_t)UINT32_MAX) {
+            set_error("conservative sweep: %lld raw entries exceed 2^32", (long long)nraw);
+            st = RG_ERR_UNSUPPORTED;
+            break;
+        }
+        if ((st = dalloc(raw_in, (size_t)nraw, s))) break;
+        if ((st = dalloc(raw_out, (size_t)nraw, s))) break;
+        if ((st = dalloc(raw_val, (size_t)nraw, s))) break;
+        walk_kernel<true><<<grid_for(base, 64), 64, 0, s>>>(P, seats, nullptr, offsets, *raw_in, *raw_out,
+                                                            *raw_val, flags);
+        *nraw_out = nraw;
+    } while (0);
+    dfree(counts, s);
+    dfree(offsets, s);
+    return st;
+}
+
+// Chunked walk (see chunk_walk_kernel).  Sets *nraw_out to -1 (and frees
+// everything) when a chunk needed more slots than it was given.
+int sweep_chunked(const SweepParams& P, const Seat* seats, const double* bbox_h, unsigned* flags,
+                  int64_t* total_dev, cudaStream_t s, int32_t** raw_in, int32_t** raw_out, double** raw_val,
+                  int64_t* nraw_out) {
+    ChunkPlan C;
+    memset(&C, 0, sizeof(C));
+    // sweep segments per chunk; RG_SWEEP_CHUNK overrides (0 walks whole lines)
+    C.ch = 32;
+    if (const char* env = getenv("RG_SWEEP_CHUNK")) C.ch = atoll(env);
+    *nraw_out = -1;
+    if (C.ch <= 0) return RG_OK;
+    int64_t chunks = 0, slots = 0;
+    for (int f = 0; f < 4; f++) {
+        const Family& F = P.fam[f];
+        const Static& S = P.st[F.st];
+        const double* bs = F.sweep_input ? bbox_h : bbox_h + 4;  // sweep grid's box
+        const double* bt = F.sweep_input ? bbox_h + 4 : bbox_h;  // static grid's box
+        double seg = fmax(bs[2] - bs[0], bs[3] - bs[1]) / (double)(F.len - 1 > 0 ? F.len - 1 : 1);
+        double dens = fmax((double)S.ncx / fmax(bt[2] - bt[0], 1e-300), (double)S.ncy / fmax(bt[3] - bt[1], 1e-300));
+        double cross = 2.0 * ceil(1.5 * seg * dens) + 2.0;
+        if (!(cross < 1e6)) cross = 1e6;
+        C.nc[f] = (F.len - 1 + C.ch - 1) / C.ch;
+        C.chunk_base[f] = chunks;
+        C.cap[f] = 2 * C.ch * (1 + (int64_t)cross) + 32;
+        C.slot_base[f] = slots;
+        chunks += F.lines * C.nc[f];
+        slots += F.lines * C.nc[f] * C.cap[f];
+    }
+    C.chunk_base[4] = chunks;
+    if (slots * 16 > (int64_t)24 << 30 || slots >= (int64_t)1 << 40) return RG_OK;  // too big: walk lines
+
+    WalkState *starts = nullptr, *ends = nullptr;
+    int64_t *counts = nullptr, *offsets = nullptr;
+    int32_t *s_in = nullptr, *s_out = nullptr;
+    double* s_val = nullptr;
+    unsigned long long* n_rep = nullptr;
+    int st = RG_OK;
+    bool overflow = false;
+    do {
+        if ((st = dalloc(&starts, (size_t)chunks, s))) break;
+        if ((st = dalloc(&ends, (size_t)chunks, s))) break;
+        if ((st = dalloc(&counts, (size_t)chunks + 1, s))) break;
+        if ((st = dalloc(&offsets, (size_t)chunks + 1, s))) break;
+        if ((st = dalloc(&n_rep, 1, s))) break;
+        if ((st = dalloc(&s_in, (size_t)slots, s))) break;
+        if ((st = dalloc(&s_out, (size_t)slots, s))) break;
+        if ((st = dalloc(&s_val, (size_t)slots, s))) break;
+        cudaMemsetAsync(n_rep, 0, sizeof(unsigned long long), s);
+        chunk_seat_kernel<<<grid_for(chunks, 128), 128, 0, s>>>(P, C, seats, starts);
+        chunk_walk_kernel<<<grid_for(chunks, 64), 64, 0, s>>>(P, C, starts, ends, counts, s_in, s_out, s_val, flags);
+        chunk_repair_kernel<<<grid_for(P.total_lines, 64), 64, 0, s>>>(P, C, starts, ends, counts, s_in, s_out,
+                                                                      s_val, flags, n_rep);
+        cudaMemsetAsync(counts + chunks, 0, sizeof(int64_t), s);
+        if ((st = exclusive_scan_i64(counts, offsets, chunks + 1, total_dev, s))) break;
+        int64_t nraw = 0;
+        unsigned fl = 0;
+        cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("conservative sweep (chunked walk): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        if ((st = check_walk_flags(fl))) break;
+        if (fl & FLAG_CAPACITY) {
+            overflow = true;
+            cudaMemsetAsync(flags, 0, sizeof(unsigned), s);
+            break;
+        }
+        if (nraw >= (int64_t)UINT32_MAX) {
+            set_error("conservative sweep: %lld raw entries exceed 2^32", (long long)nraw);
+            st = RG_ERR_UNSUPPORTED;
+            break;
+        }
+        if ((st = dalloc(raw_in, (size_t)nraw, s))) break;
+        if ((st = dalloc(raw_out, (size_t)nraw, s))) break;
+        if ((st = dalloc(raw_val, (size_t)nraw, s))) break;
+        chunk_compact_kernel<<<grid_for(chunks * 32, 256), 256, 0, s>>>(C, counts, offsets, s_in, s_out, s_val,
+                                                                        *raw_in, *raw_out, *raw_val);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("conservative sweep (compaction): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        *nraw_out = nraw;
+    } while (0);
+    dfree(starts, s);
+    dfree(ends, s);
+    dfree(counts, s);
+    dfree(offsets, s);
+    dfree(n_rep, s);
+    dfree(s_in, s);
+    dfree(s_out, s);
+    dfree(s_val, s);
+    if (overflow) *nraw_out = -1;
+    return st;
+}
+
+}  // namespace
+
 int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64_t nyi,
                           const double* xo, const double* yo, int64_t nxo, int64_t nyo,
                           const double* w_in, cudaStream_t s, rg_weights_s* W) {
@@ -873,11 +1266,12 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
     int st = RG_OK;
     double* area_in = nullptr;
     double* bbox_d = nullptr;
+    double* bbox_part = nullptr;
     Edge* edges[2] = {nullptr, nullptr};
     int32_t* bptr[2] = {nullptr, nullptr};
     int32_t* bitems[2] = {nullptr, nullptr};
     Seat* seats = nullptr;
-    int64_t *counts = nullptr, *offsets = nullptr, *total_dev = nullptr;
+    int64_t* total_dev = nullptr;
     unsigned* flags = nullptr;
     int32_t *raw_in = nullptr, *raw_out = nullptr;
     double* raw_val = nullptr;
@@ -892,11 +1286,14 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
         if ((st = dalloc(&area_in, (size_t)n_in, s))) break;
         if ((st = cell_area_2d(xi, yi, nxi, nyi, area_in, s))) break;
         if ((st = dalloc(&bbox_d, 8, s))) break;
+        if ((st = dalloc(&bbox_part, 8 * 256, s))) break;
         if ((st = dalloc(&flags, 1, s))) break;
         if ((st = dalloc(&total_dev, 1, s))) break;
         cudaMemsetAsync(flags, 0, sizeof(unsigned), s);
-        bbox_kernel<<<1, 256, 0, s>>>(xi, yi, nxi * nyi, bbox_d);
-        bbox_kernel<<<1, 256, 0, s>>>(xo, yo, nxo * nyo, bbox_d + 4);
+        bbox_partial<<<256, 256, 0, s>>>(xi, yi, nxi * nyi, bbox_part);
+        bbox_combine<<<1, 32, 0, s>>>(bbox_part, 256, bbox_d);
+        bbox_partial<<<256, 256, 0, s>>>(xo, yo, nxo * nyo, bbox_part + 4 * 256);
+        bbox_combine<<<1, 32, 0, s>>>(bbox_part + 4 * 256, 256, bbox_d + 4);
         double bbox_h[8];
         cudaMemcpyAsync(bbox_h, bbox_d, sizeof(bbox_h), cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
@@ -934,41 +1331,15 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
         P.ncy_out = ncy_out;
 
         if ((st = dalloc(&seats, (size_t)base, s))) break;
-        if ((st = dalloc(&counts, (size_t)base + 1, s))) break;
-        if ((st = dalloc(&offsets, (size_t)base + 1, s))) break;
         seat_kernel<<<grid_for(base * 32, 128), 128, 0, s>>>(P, seats, flags);
-        walk_kernel<false><<<grid_for(base, 64), 64, 0, s>>>(P, seats, counts, nullptr, nullptr, nullptr,
-                                                             nullptr, flags);
-        cudaMemsetAsync(counts + base, 0, sizeof(int64_t), s);
-        if ((st = exclusive_scan_i64(counts, offsets, base + 1, total_dev, s))) break;
         int64_t nraw = 0;
+        if ((st = sweep_chunked(P, seats, bbox_h, flags, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw)))
+            break;
+        if (nraw < 0) {
+            // a chunk overflowed its slots: walk whole lines instead
+            if ((st = sweep_lines(P, seats, flags, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw))) break;
+        }
         unsigned fl = 0;
-        cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
-        e = cudaStreamSynchronize(s);
-        if (e != cudaSuccess) {
-            set_error("build_conservative_2d (count walk): %s", cudaGetErrorString(e));
-            st = RG_ERR_CUDA;
-            break;
-        }
-        if (fl & (FLAG_WALK_CAP | FLAG_SEAT_OUTSIDE)) {
-            set_error("conservative sweep: %s",
-                      (fl & FLAG_WALK_CAP) ? "a grid line exceeded its step cap (degenerate grids?)"
-                                           : "a grid line starting inside the grid boundary could "
-                                             "not be located in any cell");
-            st = RG_ERR_WALK;
-            break;
-        }
-        if (nraw >= (int64_t)UINT32_MAX) {
-            set_error("conservative sweep: %lld raw entries exceed 2^32", (long long)nraw);
-            st = RG_ERR_UNSUPPORTED;
-            break;
-        }
-        if ((st = dalloc(&raw_in, (size_t)nraw, s))) break;
-        if ((st = dalloc(&raw_out, (size_t)nraw, s))) break;
-        if ((st = dalloc(&raw_val, (size_t)nraw, s))) break;
-        walk_kernel<true><<<grid_for(base, 64), 64, 0, s>>>(P, seats, nullptr, offsets, raw_in, raw_out,
-                                                            raw_val, flags);
         // merge
         if ((st = dalloc(&skey, (size_t)nraw, s))) break;
         cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
@@ -1019,14 +1390,13 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
 
     dfree(area_in, s);
     dfree(bbox_d, s);
+    dfree(bbox_part, s);
     for (int k = 0; k < 2; k++) {
         dfree(edges[k], s);
         dfree(bptr[k], s);
         dfree(bitems[k], s);
     }
     dfree(seats, s);
-    dfree(counts, s);
-    dfree(offsets, s);
     dfree(total_dev, s);
     dfree(flags, s);
     dfree(raw_in, s);

@@ -432,3 +432,119 @@ def test_apply_from_host_buffers(rg):
               ctypes.c_void_p(out64.ctypes.data), _lib.RG_F64, 37, _lib.RG_ACC_EXACT, 8, s)
     torch.cuda.synchronize()
     assert_same(out64, oracle.apply(ii, oo, vv, v64, 96 * 96))
+
+
+@pytest.mark.parametrize("chunk", ["0", "1", "3", "7"])
+def test_walk_chunking_is_exact(rg, chunk, monkeypatch):
+    """Whole-line walks (0) and short chunks (many seats, many repairs) give
+    the same bits as the default chunked walk and the oracle."""
+    monkeypatch.setenv("RG_SWEEP_CHUNK", chunk)
+    c = CURVI.case("curvi33")
+    w = rg.weights(c.tuple("ci"), c.tuple("co"), method="conservative")
+    assert_weights_same(w, c.weights())
+    k = KNOWN.case("c2d_9")  # exact 180-degree rotation: vertices on edges
+    w = rg.weights(k.tuple("ci"), k.tuple("co"), method="conservative", perturb=False)
+    assert_weights_same(w, k.weights())
+    gi = distorted(257, 0.25, 0.02)
+    rng = np.random.default_rng(42)
+    gop = tuple(rng.normal(a, np.ptp(a) * 1e-9) for a in rect(193, -1.05, 1.05))
+    exp = oracle.weights_conservative_2d(gi, gop)
+    got = rg.build_conservative_2d(gi, gop).export_numpy()
+    for g, e in zip(got, exp):
+        assert_same(g, e)
+
+
+def _local_coo(rng, n0_in, n1_in, n0_out, n1_out, per_row=(1, 9), empty=0.0, spread=None):
+    """Entries of a 2D-to-2D weights matrix whose output cell (i, j) reads a
+    small neighbourhood of the corresponding input cell (or, with `spread`,
+    `spread` random cells anywhere in the input)."""
+    ii, oo = [], []
+    for o in range(n0_out * n1_out):
+        if rng.random() < empty:
+            continue
+        i, j = divmod(o, n1_out)
+        ci = int(i * n0_in / n0_out)
+        cj = int(j * n1_in / n1_out)
+        if spread:
+            cells = rng.choice(n0_in * n1_in, size=spread, replace=False)
+        else:
+            k = int(rng.integers(*per_row))
+            di = rng.integers(-1, 2, k)
+            dj = rng.integers(-2, 3, k)
+            cells = np.unique(np.clip(ci + di, 0, n0_in - 1) * n1_in + np.clip(cj + dj, 0, n1_in - 1))
+        ii.extend(cells.tolist())
+        oo.extend([o] * len(cells))
+    ii = np.asarray(ii, dtype=np.int64)
+    oo = np.asarray(oo, dtype=np.int64)
+    vv = rng.uniform(0.1, 1.0, ii.size)
+    return ii, oo, vv
+
+
+@pytest.mark.parametrize(
+    "case",
+    ["vec", "vec_tail4", "scalar_odd", "unaligned", "long_lists", "huge_tile", "no_shape", "empty_rows"])
+@pytest.mark.parametrize("stack", [1, 7, 64])
+def test_fast_apply_paths(rg, case, stack):
+    """Every branch of the float32 fast apply against the oracle's float64
+    apply: sector lists (n_in % 8 == 0 and == 4, where the last sector's
+    second half lies past the slice), cell lists (n_in % 4 != 0, unaligned
+    input), tiles whose lists overflow into the direct gathers, unknown
+    output shape (row tiles) and rows without entries.  float32 accumulation
+    with FMA is checked against its forward error bound."""
+    import torch
+
+    from regridding_gb300._device import DeviceWeights
+
+    rng = np.random.default_rng([len(case), sum(map(ord, case)), stack])
+    n0_in, n1_in, n0_out, n1_out = 40, 48, 30, 37
+    kw = {}
+    if case == "scalar_odd":
+        n1_in = 47
+    if case == "long_lists":
+        kw = {"spread": 6}
+    if case == "huge_tile":
+        n0_in, n1_in = 100, 64
+    if case == "empty_rows":
+        kw = {"empty": 0.4}
+    ii, oo, vv = _local_coo(rng, n0_in, n1_in, n0_out, n1_out, **kw)
+    n_in = n0_in * n1_in
+    if case == "vec_tail4":
+        n_in = 1796  # n_in % 8 == 4; make sure the last cell is read
+        ii = np.minimum(ii, n_in - 1)
+        ii[-1] = n_in - 1
+        key = np.unique(oo * n_in + ii)
+        oo, ii = key // n_in, key % n_in
+        vv = rng.uniform(0.1, 1.0, ii.size)
+    if case == "huge_tile":
+        # one output cell reading 5000 inputs: its tile has more entries than
+        # the tile sorter holds and takes the direct gathers
+        extra = rng.choice(n_in, size=5000, replace=False)
+        keep = oo != 5
+        ii = np.concatenate([ii[keep], extra])
+        oo = np.concatenate([oo[keep], np.full(5000, 5)])
+        vv = np.concatenate([vv[keep], rng.uniform(0.1, 1.0, 5000) / 1000])
+    n_out = n0_out * n1_out
+    shape = None if case == "no_shape" else (n0_out, n1_out)
+    dw = DeviceWeights.from_coo(ii, oo, vv, n_in, n_out, shape)
+    vals = rng.uniform(0.5, 2.0, (stack, n_in)).astype(np.float32)
+    if case == "unaligned":
+        buf = torch.empty(stack * n_in + 1, dtype=torch.float32, device="cuda")
+        d_vals = buf[1:].view(stack, n_in)
+        d_vals.copy_(torch.from_numpy(vals))
+        assert d_vals.data_ptr() % 16 != 0
+    else:
+        d_vals = torch.from_numpy(vals).cuda()
+    got = dw.apply(d_vals, accumulate="fast").cpu().numpy()
+    exp = oracle.apply(ii, oo, vv, vals.astype(np.float64), n_out)
+    assert got.dtype == np.float32 and got.shape == (stack, n_out)
+    # forward error bound of a float32 FMA chain of k terms with weights
+    # rounded to float32: (k + 2) u sum|w x|, u = 2^-24
+    k = np.bincount(oo, minlength=n_out)
+    bound = (k + 2) * 2.0**-24 * oracle.apply(ii, oo, np.abs(vv), np.abs(vals).astype(np.float64), n_out)
+    assert np.all(np.abs(got - exp) <= bound), np.max(np.abs(got - exp) / np.maximum(bound, 1e-300))
+    if case == "empty_rows":
+        empty = np.setdiff1d(np.arange(n_out), oo)
+        assert empty.size > 0 and np.all(got[:, empty] == 0)
+    # applying twice (lists already built) gives the same bits
+    again = dw.apply(d_vals, accumulate="fast").cpu().numpy()
+    assert_same(again, got)

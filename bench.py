@@ -38,6 +38,7 @@ METRIC = "build cells/s; apply HBM GB/s; served req/s + p50/p99 vs plain GPU pat
 STACK = 64
 N_IN = 2049
 N_OUT = 1537
+SERVE_RATE = 500.0
 PEAK_FALLBACK_GBS = 6800.0
 
 
@@ -212,6 +213,119 @@ def run_quick(args, local):
                       "GB_per_s": b / statistics.mean(per) / 1e9}), flush=True)
 
 
+def run_serving(args, torch):
+    """The served stream (Poisson arrivals at SERVE_RATE req/s, grid sides
+    log-uniform in [128, 2048] cells, 70 % of requests on 32 resident grids,
+    30 % bringing a new grid, stacks of 1, 8 or 64 float32 slices, 80 GB HBM
+    budget) through RegridServer, against the plain path that serves the same
+    requests one call at a time."""
+    import oracle
+    from regridding_gb300 import workloads
+    from regridding_gb300.serving import RegridServer, regrid_plain
+
+    n_req = args.serve_requests
+    t_gen = time.perf_counter()
+    cached, reqs = workloads.served_stream(n_req, rate=SERVE_RATE)
+    t_gen = time.perf_counter() - t_gen
+    cells = lambda g: (g[0].shape[0] - 1) * (g[0].shape[1] - 1)
+    max_in = max(cells(r["pair"][0]) * r["stack"] for r in reqs)
+    max_out = max(cells(r["pair"][1]) * r["stack"] for r in reqs)
+    rng = np.random.default_rng(7)
+    pool = torch.empty(max_in, dtype=torch.float32, pin_memory=True)
+    pool.copy_(torch.from_numpy(rng.lognormal(3, 1, max_in).astype(np.float32)))
+    sinks = [torch.empty(max_out, dtype=torch.float32, pin_memory=True) for _ in range(4)]
+
+    def values(r):
+        return pool[:cells(r["pair"][0]) * r["stack"]].view(r["stack"], -1)
+
+    def sink(i, r):
+        return sinks[i % len(sinks)][:cells(r["pair"][1]) * r["stack"]].view(r["stack"], -1)
+
+    def percentiles(lat):
+        lat = np.sort(np.asarray(lat)) * 1e3
+        return round(float(np.percentile(lat, 50)), 3), round(float(np.percentile(lat, 99)), 3)
+
+    out = {"requests": n_req, "offered_rate": SERVE_RATE, "stream_generation_s": round(t_gen, 2),
+           "slots": args.serve_slots,
+           "grids": "clients send output grids that already carry their 1e-9 jitter; server and plain path "
+                    "both run with perturb=False"}
+    for mode in ("poisson", "saturated"):
+        # a fresh server per pass: the 32 resident grids are built before the
+        # stream starts, every new grid of the stream is built during it
+        with RegridServer(hbm_budget=80e9, slots=args.serve_slots, max_batch_stack=64, perturb=False) as srv:
+            warm = [srv.submit(gi, go, np.zeros((1, cells(gi)), np.float32)) for gi, go in cached]
+            for f in warm:
+                f.result()
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            futs = []
+            for i, r in enumerate(reqs):
+                t_arr = t0 + (r["t"] if mode == "poisson" else 0.0)
+                if mode == "poisson":
+                    delay = t_arr - time.perf_counter()
+                    if delay > 0:
+                        time.sleep(delay)
+                futs.append(srv.submit(*r["pair"], values(r), out=sink(i, r), t_arrival=t_arr))
+            for f in futs:
+                f.result()
+            t_end = max(f.request.t_done for f in futs)
+            lat = [f.request.t_done - f.request.t_arrival for f in futs]
+            p50, p99 = percentiles(lat)
+            new = [f.request.t_done - f.request.t_arrival for f, r in zip(futs, reqs) if r["cached"] < 0]
+            old = [f.request.t_done - f.request.t_arrival for f, r in zip(futs, reqs) if r["cached"] >= 0]
+            out[mode] = {"req_per_s": round(n_req / (t_end - t0), 1), "p50_ms": p50, "p99_ms": p99,
+                         "p50_p99_ms_resident_grid": percentiles(old), "p50_p99_ms_new_grid": percentiles(new),
+                         "mean_batch": round(float(np.mean([f.request.batch for f in futs])), 2),
+                         "server": {k: v for k, v in srv.stats().items() if k != "budget"}}
+    torch.cuda.synchronize()
+    # plain path: the same requests one call at a time (build, copy in, apply, copy out, free)
+    for mode in ("plain_per_call", "plain_cached"):
+        store = {}
+        t0 = time.perf_counter()
+        lat = []
+        from regridding_gb300 import _device
+        for i, r in enumerate(reqs):
+            s = time.perf_counter()
+            gi, go = r["pair"]
+            if mode == "plain_per_call" or r["cached"] < 0:
+                regrid_plain(gi, go, values(r), out=sink(i, r), perturb=False)
+            else:
+                dw = store.get(r["cached"])
+                if dw is None:
+                    dw = store[r["cached"]] = _device.build_conservative_2d(gi, go)
+                v = values(r).cuda(non_blocking=True)
+                o = dw.apply(v, accumulate="fast")
+                sink(i, r).copy_(o)
+            lat.append(time.perf_counter() - s)
+        torch.cuda.synchronize()
+        t = time.perf_counter() - t0
+        p50, p99 = percentiles(lat)
+        out[mode] = {"req_per_s": round(n_req / t, 1), "service_p50_ms": p50, "service_p99_ms": p99}
+        for dw in store.values():
+            dw.free()
+    out["speedup_saturated_vs_plain_per_call"] = round(out["saturated"]["req_per_s"] /
+                                                        out["plain_per_call"]["req_per_s"], 2)
+    # what the upstream's default server-side jitter would add per new grid
+    # (numpy normal() on the host, one core)
+    from regridding_gb300 import _util
+    news = [r for r in reqs if r["cached"] < 0][:20]
+    s = time.perf_counter()
+    for r in news:
+        _util.normalize_input_output_coordinates(*r["pair"], None, None, perturb=True, seed=42)
+    out["host_jitter_ms_per_new_grid"] = round((time.perf_counter() - s) / len(news) * 1e3, 2)
+    # weights of the smallest new grid of the stream against the oracle (float64)
+    r = min((r for r in reqs if r["cached"] < 0), key=lambda r: cells(r["pair"][0]))
+    from regridding_gb300 import _device
+    gi, go = r["pair"]
+    got = _device.build_conservative_2d(gi, go).export_numpy()
+    exp = oracle.weights_conservative_2d(gi, go)
+    same = all(np.array_equal(a, b) for a, b in zip(got, exp))
+    rel = 0.0 if same else float(np.max(np.abs(got[2] - exp[2]) / np.abs(exp[2]))) if got[2].shape == exp[2].shape \
+        else float("inf")
+    out["weights_check"] = {"grid_cells": cells(r["pair"][0]), "bit_identical": same, "max_rel_err": rel}
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -306,6 +420,15 @@ def run_ours(args, world, rank, local):
     apply_exact()
     torch.cuda.synchronize()
     rel = float(((out32.double() - out64).abs() / out64.abs().clamp_min(1e-30)).max().item())
+    # conservation: the output total against the input weighted by the
+    # fraction of each input cell the output grid covers (the transposed
+    # apply of ones), per slice, relative to the input total
+    ones = torch.ones((1, n_out_cells), dtype=torch.float64, device="cuda")
+    covered = dw.apply(ones, transpose=True, accumulate="exact")[0]
+    vin64 = values.double()
+    cons = ((out64.sum(1) - vin64 @ covered).abs() / vin64.sum(1)).max().item()
+    cons_uncovered = float(1.0 - (vin64 @ covered).sum().item() / vin64.sum().item())
+    del vin64, ones, covered
 
     # --- CPU baseline: the oracle (C restatement of the upstream loops, all cores)
     cpu = None
@@ -358,12 +481,15 @@ def run_ours(args, world, rank, local):
                             "ms": round(statistics.mean(per64) * 1e3, 4),
                             "note": "bit-identical to the upstream float64 apply"},
         "apply_f32_max_rel_err_vs_f64": rel,
+        "conservation": {"max_rel_err_exact_f64": cons, "input_fraction_outside_output_grid": cons_uncovered},
         "build": {"cells_per_s": round((n_in_cells + n_out_cells) / (min(build_ms) / 1e3), 0),
                   "ms": [round(v, 2) for v in build_ms], "nnz": nnz},
         "find_indices_2d": {"points_per_s": round(px.numel() / (min(fi_ms) / 1e3), 0),
                             "ms": [round(v, 3) for v in fi_ms], "points": int(px.numel()),
                             "outside": n_outside},
     }
+    if rank == 0 and args.serve_requests > 0:
+        line["serving"] = run_serving(args, torch)
     if rank == 0:
         print(json.dumps(line), flush=True)
 
@@ -443,6 +569,8 @@ def main(argv=None):
     p.add_argument("--n-in", type=int, default=N_IN)
     p.add_argument("--n-out", type=int, default=N_OUT)
     p.add_argument("--stack", type=int, default=STACK)
+    p.add_argument("--serve-requests", type=int, default=1000, help="requests of the served stream (0: skip)")
+    p.add_argument("--serve-slots", type=int, default=8)
     args = p.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

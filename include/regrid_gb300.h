@@ -92,7 +92,13 @@ int rg_weights_from_coo(const int64_t* d_in, const int64_t* d_out, const double*
 int rg_weights_info(rg_weights w, int64_t* nnz, int64_t* n_in, int64_t* n_out);
 
 /* Record the 2D shape of the output cells (rows of the matrix) so the apply
- * can tile them in two dimensions.  Optional. */
+ * can tile them in two dimensions.  Optional; the shape cannot change once a
+ * fast float32 apply has run with the handle (RG_ERR_ARG).
+ *
+ * Handles may be shared between threads and streams: the state an apply
+ * makes on first use (float32 weights, tile lists, transposed CSR) is made
+ * under a per-handle lock and completed before other calls can see it.
+ * Freeing a handle while another call uses it is the caller's error. */
 int rg_weights_set_output_shape(rg_weights w, int64_t n0, int64_t n1);
 
 /* Entries in the upstream saved layout: unique (input, output) pairs sorted by
@@ -227,6 +233,19 @@ int rg_transpose_conservative_scale(const int64_t* d_in, const int64_t* d_out, c
                                     int64_t nnz, const double* d_vol_in, int64_t n_in,
                                     const double* d_vol_out, int64_t n_out, const double* d_w_in,
                                     double* d_result, rg_stream_t stream);
+
+/* Device bytes currently held by a handle: the CSR plus whatever state
+ * applies have made on first use (float32 weights, tile lists, transposed
+ * CSR).  Used by caches that account weights against an HBM budget.  No
+ * upstream counterpart. */
+int rg_weights_device_bytes(rg_weights w, int64_t* bytes);
+
+/* 64-bit hash of a host byte range (seeded), for cache keys of grids.  Host
+ * code only; ranges above 4 MiB are hashed in 1 MiB segments on up to 8
+ * host threads (the value does not depend on the thread count).  Not
+ * cryptographic.  No upstream counterpart (the served form keys its weights
+ * cache by grid hash). */
+int rg_hash64(const void* h_data, int64_t nbytes, uint64_t seed, uint64_t* h_out);
 
 #ifdef __cplusplus
 }

@@ -66,7 +66,7 @@ def build(force: bool = False, verbose: bool = False) -> str:
         objs = list(ex.map(compile_one, srcs))
     if force or _stale(LIB, objs):
         tmp = LIB + ".tmp"
-        cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs]
+        cmd = [exe, *ARCH, "-shared", "-o", tmp, *objs, "-lpthread"]
         res = subprocess.run(cmd, capture_output=True, text=True)
         if res.returncode != 0:
             raise RuntimeError(f"nvcc link failed:\n{res.stdout}\n{res.stderr}")

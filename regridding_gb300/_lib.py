@@ -50,6 +50,8 @@ SIGNATURES = {
     "rg_multilinear_1d": [_P, _I, _I, _P, _P, _I, _I, _I, _P, _I, _C, _P, _P, _P, ctypes.POINTER(_I), _P],
     "rg_conservative_1d": [_P, _I, _I, _P, _I, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P],
     "rg_transpose_conservative_scale": [_P, _P, _P, _I, _P, _I, _P, _I, _P, _P, _P],
+    "rg_weights_device_bytes": [_P, ctypes.POINTER(_I)],
+    "rg_hash64": [_P, _I, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
 }
 
 _lock = threading.Lock()

@@ -123,7 +123,7 @@ int launch(const int64_t* row_ptr, const int32_t* col, const Tw* val, int64_t n_
     return RG_OK;
 }
 
-int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, float** val32,
+int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, const float* val32,
               int64_t nnz, int64_t n_rows, int64_t n_cols, int64_t shape0, int64_t shape1,
               const void* vin, int dtype_in, void* vout, int dtype_out, int64_t stack, int acc,
               cudaStream_t s) {
@@ -152,38 +152,58 @@ int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, flo
         return launch<double, double, 2, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols, vout,
                                                  stack, s);
     }
-    // float32 output, fast: weights rounded to float once (lazily cached)
-    if (*val32 == nullptr && nnz > 0) {
-        RG_TRY(dalloc(val32, (size_t)nnz, s));
-        to_f32<<<grid_for(nnz, 256) > 8192 ? 8192 : grid_for(nnz, 256), 256, 0, s>>>(val, *val32, nnz);
-    }
+    // float32 output, fast: the weights rounded to float once (made by the caller)
     if (dtype_in == RG_F32)
-        return launch<float, float, 2, float>(row_ptr, col, *val32, n_rows, shape0, shape1, vin, n_cols, vout,
+        return launch<float, float, 2, float>(row_ptr, col, val32, n_rows, shape0, shape1, vin, n_cols, vout,
                                               stack, s);
-    return launch<double, float, 2, float>(row_ptr, col, *val32, n_rows, shape0, shape1, vin, n_cols, vout,
+    return launch<double, float, 2, float>(row_ptr, col, val32, n_rows, shape0, shape1, vin, n_cols, vout,
                                            stack, s);
 }
 
 }  // namespace
 
-int apply_tiled(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int tiled_lists_for(rg_weights_s* W, const float* vin, cudaStream_t s, int* g, bool* made);
+int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int ensure_transposed(rg_weights_s* W, cudaStream_t s);
 
+// Every apply goes through here.  The per-handle state an apply needs beyond
+// the CSR (the transposed CSR, the float32 copy of the weights, the warp-tile
+// lists) is made on first use under the handle's mutex and finished (the
+// stream synchronised) before the lock is released, so calls from other
+// threads and streams only ever see complete state.
 int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_in, void* vout,
                   int dtype_out, int64_t stack, int acc, cudaStream_t s) {
-    if (!transposed && acc == RG_ACC_FAST && dtype_in == RG_F32 && dtype_out == RG_F32 && stack > 0 &&
-        W->n_out > 0 && W->nnz > 0) {
-        // the bandwidth path: float32 in and out, gather lists staged in shared memory
-        if (W->val32 == nullptr) {
-            RG_TRY(dalloc(&W->val32, (size_t)W->nnz, s));
-            to_f32<<<grid_for(W->nnz, 256) > 8192 ? 8192 : grid_for(W->nnz, 256), 256, 0, s>>>(W->val, W->val32,
-                                                                                              W->nnz);
+    RG_CHECK(dtype_in == RG_F32 || dtype_in == RG_F64, RG_ERR_ARG, "apply: bad input dtype");
+    RG_CHECK(dtype_out == RG_F32 || dtype_out == RG_F64, RG_ERR_ARG, "apply: bad output dtype");
+    RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST, RG_ERR_ARG, "apply: bad accumulation mode");
+    if (stack <= 0) return RG_OK;
+    // the bandwidth path: float32 in and out, gather lists staged in shared memory
+    const bool tiled = !transposed && acc == RG_ACC_FAST && dtype_in == RG_F32 && dtype_out == RG_F32 &&
+                       W->n_out > 0 && W->nnz > 0;
+    const bool need32 = acc == RG_ACC_FAST && dtype_out == RG_F32 && W->nnz > 0;
+    int g = 0;
+    {
+        std::lock_guard<std::mutex> lock(W->mu);
+        bool made = false;
+        if (transposed && W->t_row_ptr == nullptr) {
+            RG_TRY(ensure_transposed(W, s));
+            made = true;
         }
-        return apply_tiled(W, (const float*)vin, (float*)vout, stack, s);
+        float** v32 = transposed ? &W->t_val32 : &W->val32;
+        if (need32 && *v32 == nullptr) {
+            RG_TRY(dalloc(v32, (size_t)W->nnz, s));
+            to_f32<<<grid_for(W->nnz, 256) > 8192 ? 8192 : grid_for(W->nnz, 256), 256, 0, s>>>(
+                transposed ? W->t_val : W->val, *v32, W->nnz);
+            made = true;
+        }
+        if (tiled) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
+        if (made) RG_CUDA(cudaStreamSynchronize(s));
     }
+    if (tiled) return apply_tiled(W, g, (const float*)vin, (float*)vout, stack, s);
     if (!transposed)
-        return apply_csr(W->row_ptr, W->col, W->val, &W->val32, W->nnz, W->n_out, W->n_in, W->out_shape0,
+        return apply_csr(W->row_ptr, W->col, W->val, W->val32, W->nnz, W->n_out, W->n_in, W->out_shape0,
                          W->out_shape1, vin, dtype_in, vout, dtype_out, stack, acc, s);
-    return apply_csr(W->t_row_ptr, W->t_col, W->t_val, &W->t_val32, W->nnz, W->n_in, W->n_out, 0, 0, vin,
+    return apply_csr(W->t_row_ptr, W->t_col, W->t_val, W->t_val32, W->nnz, W->n_in, W->n_out, 0, 0, vin,
                      dtype_in, vout, dtype_out, stack, acc, s);
 }
 

@@ -447,16 +447,28 @@ int prepare_tiled(rg_weights_s* W, int grain, cudaStream_t s) {
     return st;
 }
 
-int apply_tiled(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
-    // sector lists need 16-byte aligned slices; tiles whose sector list
-    // exceeds 32 fall back to the cell lists of the scalar kernel
+// Which lists the fast apply of `vin` uses (*g = 1: sector lists and the
+// vector kernel; 0: cell lists and the scalar kernel), building them if they
+// do not exist yet (*made set).  Sector lists need 16-byte aligned slices;
+// when some tile's sector list exceeds 32 the cell lists are used instead.
+// The caller holds the handle's lock.
+int tiled_lists_for(rg_weights_s* W, const float* vin, cudaStream_t s, int* g, bool* made) {
     bool vec = W->n_in % 4 == 0 && ((uintptr_t)vin & 15) == 0;
     if (vec) {
+        if (!W->tiled_ready[1]) *made = true;
         RG_TRY(prepare_tiled(W, 8, s));
         vec = W->t_gmax[1] <= 32;
     }
-    const int g = vec ? 1 : 0;
-    if (!vec) RG_TRY(prepare_tiled(W, 1, s));
+    if (!vec) {
+        if (!W->tiled_ready[0]) *made = true;
+        RG_TRY(prepare_tiled(W, 1, s));
+    }
+    *g = vec ? 1 : 0;
+    return RG_OK;
+}
+
+int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+    const bool vec = g == 1;
     const TileShape T = tile_shape(W);
     const int64_t wtiles = W->t_tiles;
     const int64_t blocks = (wtiles + WARPS - 1) / WARPS;

@@ -2,6 +2,8 @@
 #include <cstdarg>
 #include <cstring>
 #include <new>
+#include <thread>
+#include <vector>
 
 #include "common.cuh"
 
@@ -137,6 +139,44 @@ int column_order(rg_weights_s* W, int32_t** row_of, uint32_t** perm, int64_t** c
     return st;
 }
 
+void free_weights(rg_weights_s* W, cudaStream_t s) {
+    dfree(W->row_ptr, s);
+    dfree(W->col, s);
+    dfree(W->val, s);
+    dfree(W->val32, s);
+    dfree(W->t_row_ptr, s);
+    dfree(W->t_col, s);
+    dfree(W->t_val, s);
+    dfree(W->t_val32, s);
+    for (int g = 0; g < 2; g++) {
+        dfree(W->t_gptr[g], s);
+        dfree(W->t_gidx[g], s);
+        dfree(W->t_slot[g], s);
+    }
+    delete W;
+}
+
+}  // namespace
+
+void init_pool_once() {
+    static std::once_flag flags[64];
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+        cudaGetLastError();
+        return;
+    }
+    std::call_once(flags[dev], [dev]() {
+        cudaMemPool_t pool;
+        if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+            uint64_t keep = POOL_KEEP_BYTES;
+            cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
+        }
+        cudaGetLastError();
+    });
+}
+
+// Build the CSC (rows = input cells) for the transposed apply; the caller
+// holds the handle's lock.
 int ensure_transposed(rg_weights_s* W, cudaStream_t s) {
     if (W->t_row_ptr) return RG_OK;
     int32_t* row_of = nullptr;
@@ -164,24 +204,6 @@ int ensure_transposed(rg_weights_s* W, cudaStream_t s) {
     return st;
 }
 
-void free_weights(rg_weights_s* W, cudaStream_t s) {
-    dfree(W->row_ptr, s);
-    dfree(W->col, s);
-    dfree(W->val, s);
-    dfree(W->val32, s);
-    dfree(W->t_row_ptr, s);
-    dfree(W->t_col, s);
-    dfree(W->t_val, s);
-    dfree(W->t_val32, s);
-    for (int g = 0; g < 2; g++) {
-        dfree(W->t_gptr[g], s);
-        dfree(W->t_gidx[g], s);
-        dfree(W->t_slot[g], s);
-    }
-    delete W;
-}
-
-}  // namespace
 }  // namespace rg
 
 using namespace rg;
@@ -294,6 +316,10 @@ int rg_weights_set_output_shape(rg_weights w, int64_t n0, int64_t n1) {
     RG_CHECK(w, RG_ERR_ARG, "rg_weights_set_output_shape: NULL handle");
     RG_CHECK(n0 * n1 == w->n_out, RG_ERR_ARG, "rg_weights_set_output_shape: %lld x %lld != %lld",
              (long long)n0, (long long)n1, (long long)w->n_out);
+    std::lock_guard<std::mutex> lock(w->mu);
+    if (w->out_shape0 == n0 && w->out_shape1 == n1) return RG_OK;
+    RG_CHECK(!w->tiled_ready[0] && !w->tiled_ready[1], RG_ERR_ARG,
+             "rg_weights_set_output_shape: the output tiling is fixed once a fast float32 apply has run");
     w->out_shape0 = n0;
     w->out_shape1 = n1;
     return RG_OK;
@@ -337,7 +363,6 @@ int rg_apply_host(rg_weights w, const void* h_vin, int dtype_in, void* h_vout, i
 int rg_apply_transpose(rg_weights w, const void* d_vout, int dtype_out, void* d_vin, int dtype_in,
                        int64_t stack, int acc, rg_stream_t stream) {
     RG_CHECK(w, RG_ERR_ARG, "rg_apply_transpose: NULL handle");
-    RG_TRY(ensure_transposed(w, (cudaStream_t)stream));
     return apply_weights(w, true, d_vout, dtype_out, d_vin, dtype_in, stack, acc, (cudaStream_t)stream);
 }
 
@@ -394,3 +419,73 @@ int rg_transpose_conservative_scale(const int64_t* d_in, const int64_t* d_out, c
 }
 
 }  // extern "C"
+
+int rg_weights_device_bytes(rg_weights w, int64_t* bytes) {
+    RG_CHECK(w && bytes, RG_ERR_ARG, "rg_weights_device_bytes: NULL argument");
+    std::lock_guard<std::mutex> lock(w->mu);
+    const int64_t nnz = w->nnz;
+    int64_t b = (w->n_out + 1) * 8 + nnz * (4 + 8);
+    if (w->val32) b += nnz * 4;
+    if (w->t_row_ptr) b += (w->n_in + 1) * 8 + nnz * (4 + 8);
+    if (w->t_val32) b += nnz * 4;
+    for (int g = 0; g < 2; g++)
+        if (w->tiled_ready[g]) b += (w->t_tiles + 1) * 8 + nnz * 2;  // list pointers + slots (lists are small)
+    *bytes = b;
+    return RG_OK;
+}
+
+// Four independent 64-bit lanes over 8-byte words (multiply, rotate,
+// multiply), folded together with the splitmix64 finaliser (Vigna).  Inputs
+// above 4 MiB are cut into 1 MiB segments hashed on up to 8 host threads and
+// combined in order, so the value does not depend on the thread count.
+// Written for speed, not for resistance to chosen inputs.
+namespace {
+inline uint64_t rotl64(uint64_t x, int r) { return (x << r) | (x >> (64 - r)); }
+inline uint64_t fin64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xbf58476d1ce4e5b9ULL;
+    z = (z ^ (z >> 27)) * 0x94d049bb133111ebULL;
+    return z ^ (z >> 31);
+}
+uint64_t hash_range(const unsigned char* p, int64_t n, uint64_t seed) {
+    const uint64_t K1 = 0x9e3779b97f4a7c15ULL, K2 = 0xd6e8feb86659fd93ULL;
+    uint64_t a[4] = {seed ^ K1, seed + K2, rotl64(seed, 17) ^ K2, ~seed};
+    const int64_t total = n;
+    while (n >= 32) {
+        uint64_t w[4];
+        memcpy(w, p, 32);
+        for (int k = 0; k < 4; k++) a[k] = rotl64((a[k] ^ w[k]) * K1, 31) * K2;
+        p += 32;
+        n -= 32;
+    }
+    uint64_t tail[4] = {0, 0, 0, 0};
+    memcpy(tail, p, (size_t)n);
+    for (int k = 0; k < 4; k++) a[k] = rotl64((a[k] ^ tail[k]) * K1, 31) * K2;
+    uint64_t h = fin64((uint64_t)total ^ seed);
+    for (int k = 0; k < 4; k++) h = fin64(h ^ a[k]);
+    return h;
+}
+}  // namespace
+
+int rg_hash64(const void* h_data, int64_t nbytes, uint64_t seed, uint64_t* h_out) {
+    RG_CHECK(h_out && nbytes >= 0 && (h_data || nbytes == 0), RG_ERR_ARG, "rg_hash64: bad argument");
+    const unsigned char* p = (const unsigned char*)h_data;
+    const int64_t SEG = 1 << 20;
+    if (nbytes <= 4 * SEG) {
+        *h_out = hash_range(p, nbytes, seed);
+        return RG_OK;
+    }
+    const int64_t nseg = (nbytes + SEG - 1) / SEG;
+    std::vector<uint64_t> part((size_t)nseg);
+    const int nthr = (int)(nseg < 8 ? nseg : 8);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; t++)
+        pool.emplace_back([&, t]() {
+            for (int64_t k = t; k < nseg; k += nthr) {
+                const int64_t len = nbytes - k * SEG < SEG ? nbytes - k * SEG : SEG;
+                part[(size_t)k] = hash_range(p + k * SEG, len, seed ^ (uint64_t)k);
+            }
+        });
+    for (auto& th : pool) th.join();
+    *h_out = hash_range((const unsigned char*)part.data(), nseg * 8, seed ^ (uint64_t)nbytes);
+    return RG_OK;
+}

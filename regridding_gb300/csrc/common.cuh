@@ -5,6 +5,7 @@
 #include <stdint.h>
 
 #include <cstdio>
+#include <mutex>
 #include <string>
 
 #include "../../include/regrid_gb300.h"
@@ -66,10 +67,19 @@ __device__ __forceinline__ double ddiv(double a, double b) { return __ddiv_rn(a,
 
 constexpr int64_t MAXSIZE = INT64_MAX;  // sys.maxsize: the upstream out-of-grid sentinel
 
+// Keep up to this many bytes of freed stream-ordered memory in the current
+// device's default pool instead of returning it to the driver at every
+// synchronisation (the pool is this process's; the setting ends with it).
+// Builds allocate and free their scratch every call; without it each build
+// maps its scratch anew.  Implemented in capi.cu; once per device.
+constexpr uint64_t POOL_KEEP_BYTES = 8ull << 30;
+void init_pool_once();
+
 // simple RAII-free device buffer helpers (stream ordered)
 template <typename T>
 int dalloc(T** p, size_t n, cudaStream_t s) {
     *p = nullptr;
+    init_pool_once();
     if (n == 0) n = 1;
     cudaError_t e = cudaMallocAsync((void**)p, n * sizeof(T), s);
     if (e != cudaSuccess) {
@@ -132,4 +142,5 @@ struct rg_weights_s {
     int32_t* t_gidx[2] = {nullptr, nullptr};   // the lists
     uint16_t* t_slot[2] = {nullptr, nullptr};  // [nnz] staged slot of each entry
     int device = 0;
+    std::mutex mu;  // guards the lazily made state above (made on first use by an apply)
 };

@@ -81,3 +81,57 @@ def cfg2_values_torch(stack: int = 64, n: int = 2048, seed: int = 0, device="cud
     v = torch.empty((stack, n * n), dtype=torch.float32, device=device)
     v.normal_(mean=3.0, std=1.0, generator=g)
     return v.exp_()
+
+
+def grid_pair(rng: np.random.Generator, side: int, jitter: bool = True):
+    """One grid pair of the batched and served configurations: an input of
+    ``side x side`` cells on [-1, 1]^2 with a random rotation in [0, 0.5) rad
+    and sinusoidal distortion of amplitude uniform(0, 0.03); a rectilinear
+    output covering uniform(0.9, 1.1) of the input extent with
+    ``round(0.75 side)`` cells per axis.  With ``jitter`` the output vertices
+    carry a normal(0, ptp * 1e-9) jitter drawn from ``rng`` (the client-side
+    form of the upstream's default perturbation: without it the two grids
+    share the vertex (0, 0) whenever both vertex counts are odd, and the
+    upstream sweep does not terminate on shared vertices).  Vertex arrays are
+    read-only."""
+    angle = rng.uniform(0, 0.5)
+    amp = rng.uniform(0, 0.03)
+    gi = distorted_grid(side + 1, angle, amp)
+    ext = rng.uniform(0.9, 1.1)
+    m = max(1, int(round(0.75 * side)))
+    go = rect_grid(m + 1, -ext, ext)
+    if jitter:
+        go = tuple(rng.normal(c, np.ptp(c) * 1e-9) for c in go)
+    for a in (*gi, *go):
+        a.setflags(write=False)
+    return gi, go
+
+
+def log_uniform_side(rng: np.random.Generator, lo: int, hi: int) -> int:
+    return int(round(np.exp(rng.uniform(np.log(lo), np.log(hi)))))
+
+
+def served_stream(n_requests: int, rate: float = 500.0, n_cached: int = 32, reuse: float = 0.7,
+                  side_lo: int = 128, side_hi: int = 2048, stacks=(1, 8, 64), seed: int = 5):
+    """The served request stream: Poisson arrivals at ``rate`` req/s, grid
+    sides log-uniform in [side_lo, side_hi] cells, a fraction ``reuse`` of the
+    requests on one of ``n_cached`` grid pairs (weights resident once built),
+    the rest on a new grid pair each, stack depths uniform over ``stacks``.
+
+    Returns (cached pairs, requests); a request is a dict with ``t`` (arrival
+    offset, s), ``pair`` (the grid pair), ``cached`` (index or -1) and
+    ``stack``."""
+    rng = np.random.default_rng(seed)
+    cached = [grid_pair(rng, log_uniform_side(rng, side_lo, side_hi)) for _ in range(n_cached)]
+    t = 0.0
+    reqs = []
+    for _ in range(n_requests):
+        t += rng.exponential(1.0 / rate)
+        stack = int(rng.choice(stacks))
+        if rng.random() < reuse:
+            k = int(rng.integers(n_cached))
+            reqs.append({"t": t, "pair": cached[k], "cached": k, "stack": stack})
+        else:
+            reqs.append({"t": t, "pair": grid_pair(rng, log_uniform_side(rng, side_lo, side_hi)), "cached": -1,
+                         "stack": stack})
+    return cached, reqs

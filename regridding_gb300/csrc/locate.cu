@@ -8,9 +8,11 @@
 // containment test (the extended winding number of geometry.py:737-829)
 // succeeds, and finally takes the lowest-index containing cell among the 3x3
 // neighbourhood, which is the exhaustive answer whenever cells do not overlap.
-// Points whose walk leaves the grid or exceeds its step cap are resolved by a
-// warp each: a lane-parallel winding test against the whole grid boundary
-// decides "outside", otherwise a lane-parallel exhaustive scan answers.
+// Points whose walk leaves the grid or exceeds its step cap are resolved by
+// the winding number of the grid boundary (from y-binned boundary edges:
+// zero means outside), and the rest by a lane-parallel exhaustive scan.  The
+// allocation-free variant keeps the older fallback, a warp per point with a
+// lane-parallel winding test over the whole boundary.
 #include <cmath>
 #include <mutex>
 
@@ -217,28 +219,218 @@ __global__ void __launch_bounds__(128)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Outside test with the grid boundary binned by y.  The extended winding
+// number of a point sums a term over boundary edges, and only edges whose
+// y-range contains the point's y give a non-zero term (a strict crossing or
+// an endpoint at that y).  Edges are binned by y with the monotone map
+// bin(v) = floor((v - ymin) * inv_h) (clamped), so an edge spanning
+// [ylo, yhi] is filed in every bin from bin(ylo) to bin(yhi) and a point at y
+// finds every edge it needs in bin(y).  The terms are +-1 and +-1/2, so their
+// sum is exact in any order.  Bins whose fill would exceed the capacity set a
+// flag and every point goes to the exhaustive scan instead.
+// ---------------------------------------------------------------------------
+
+struct YBins {
+    double ymin, ymax, inv_h;
+    int nbins;
+};
+
+__device__ __forceinline__ int ybin(const YBins& b, double v) {
+    double f = floor(dmul(dsub(v, b.ymin), b.inv_h));
+    if (!(f >= 0)) return 0;
+    if (f >= (double)(b.nbins - 1)) return b.nbins - 1;
+    return (int)f;
+}
+
+// one block: y-range of the boundary vertices -> bin parameters
+__global__ void ybins_params(G2 g, int64_t nb, int nbins, YBins* out) {
+    __shared__ double smin[256], smax[256];
+    double lo = INFINITY, hi = -INFINITY;
+    for (int64_t v = threadIdx.x; v < nb; v += blockDim.x) {
+        double bx, by;
+        bvertex(g, v, &bx, &by);
+        lo = fmin(lo, by);
+        hi = fmax(hi, by);
+    }
+    smin[threadIdx.x] = lo;
+    smax[threadIdx.x] = hi;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+        if ((int)threadIdx.x < o) {
+            smin[threadIdx.x] = fmin(smin[threadIdx.x], smin[threadIdx.x + o]);
+            smax[threadIdx.x] = fmax(smax[threadIdx.x], smax[threadIdx.x + o]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+        YBins b;
+        b.ymin = smin[0];
+        b.ymax = smax[0];
+        b.nbins = nbins;
+        double ext = dsub(b.ymax, b.ymin);
+        b.inv_h = ext > 0 && isfinite(ext) ? ddiv((double)nbins, ext) : 0.0;
+        *out = b;
+    }
+}
+
+// PASS 0 counts the bins of every boundary edge; PASS 1 files the edges
+template <int PASS>
+__global__ void ybins_fill(G2 g, int64_t nb, const YBins* __restrict__ bp, unsigned* __restrict__ counts,
+                           const int64_t* __restrict__ ptr, int32_t* __restrict__ items, int64_t cap,
+                           unsigned* __restrict__ overflow) {
+    const YBins b = *bp;
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nb; e += (int64_t)gridDim.x * blockDim.x) {
+        double ax, ay, bx, by;
+        bvertex(g, e == 0 ? nb - 1 : e - 1, &ax, &ay);
+        bvertex(g, e, &bx, &by);
+        int b0 = ybin(b, fmin(ay, by)), b1 = ybin(b, fmax(ay, by));
+        if (!(ay == ay) || !(by == by)) {  // NaN vertex: file it everywhere
+            b0 = 0;
+            b1 = b.nbins - 1;
+        }
+        for (int k = b0; k <= b1; k++) {
+            unsigned pos = atomicAdd(&counts[k], 1u);
+            if (PASS == 1) {
+                int64_t at = ptr[k] + pos;
+                if (at < cap) items[at] = (int32_t)e;
+                else atomicOr(overflow, 1u);
+            }
+        }
+    }
+}
+
+// thread per point the walk could not place: winding number from its bin;
+// zero -> outside, otherwise the point goes to the exhaustive scan
+__global__ void __launch_bounds__(128)
+    locate_resolve_kernel(G2 g, int64_t nb, const double* __restrict__ px, const double* __restrict__ py,
+                          const int64_t* __restrict__ fails, const unsigned long long* __restrict__ nfail,
+                          const YBins* __restrict__ bp, const int64_t* __restrict__ ptr,
+                          const int32_t* __restrict__ items, const int64_t* __restrict__ total,
+                          const unsigned* __restrict__ overflow, int64_t cap, int64_t* __restrict__ hard,
+                          unsigned long long* __restrict__ nhard, int64_t* __restrict__ oi,
+                          int64_t* __restrict__ oj) {
+    const unsigned long long nf = *nfail;
+    const bool usable = *overflow == 0 && *total <= cap;
+    const YBins b = *bp;
+    for (unsigned long long w = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; w < nf;
+         w += (unsigned long long)gridDim.x * blockDim.x) {
+        const int64_t k = fails[w];
+        const double x = px[k], y = py[k];
+        bool inside = true;  // unknown: scan
+        if (usable) {
+            if (!(y >= b.ymin && y <= b.ymax)) {
+                inside = false;
+            } else {
+                const int bin = ybin(b, y);
+                double wn = 0;
+                for (int64_t q = ptr[bin]; q < ptr[bin + 1]; q++) {
+                    const int64_t e = items[q];
+                    double ax, ay, bx, by;
+                    bvertex(g, e == 0 ? nb - 1 : e - 1, &ax, &ay);
+                    bvertex(g, e, &bx, &by);
+                    wn += wterm(x, y, ax, ay, bx, by);
+                }
+                inside = wn != 0;
+            }
+        }
+        if (inside) {
+            hard[atomicAdd(nhard, 1ull)] = k;
+        } else {
+            oi[k] = MAXSIZE;
+            oj[k] = MAXSIZE;
+        }
+    }
+}
+
+// warp per point inside the boundary that the walk missed: lowest-index
+// containing cell by exhaustive scan (MAXSIZE if none)
+__global__ void __launch_bounds__(128)
+    locate_exhaustive_kernel(G2 g, const double* __restrict__ px, const double* __restrict__ py,
+                             const int64_t* __restrict__ hard, const unsigned long long* __restrict__ nhard,
+                             int64_t* __restrict__ oi, int64_t* __restrict__ oj) {
+    const int lane = threadIdx.x & 31;
+    const unsigned long long nh = *nhard;
+    for (unsigned long long w = (blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x) >> 5; w < nh;
+         w += ((unsigned long long)gridDim.x * blockDim.x) >> 5) {
+        const int64_t k = hard[w];
+        const double x = px[k], y = py[k];
+        int64_t ri = MAXSIZE, rj = MAXSIZE;
+        const int64_t ncy = g.ny - 1, ncells = (g.nx - 1) * ncy;
+        for (int64_t base = 0; base < ncells; base += 32) {
+            const int64_t c = base + lane;
+            const bool hit = c < ncells && contains(g, c / ncy, c % ncy, x, y);
+            const unsigned m = __ballot_sync(0xffffffffu, hit);
+            if (m) {
+                const int64_t cc = base + __ffs(m) - 1;
+                ri = cc / ncy;
+                rj = cc % ncy;
+                break;
+            }
+        }
+        if (lane == 0) {
+            oi[k] = ri;
+            oj[k] = rj;
+        }
+    }
+}
+
 }  // namespace
 
 int locate_2d_walk(const double* x, const double* y, int64_t nx, int64_t ny, const double* px,
                    const double* py, int64_t n, int64_t* oi, int64_t* oj, cudaStream_t s) {
     if (n <= 0) return RG_OK;
-    int64_t* fails = nullptr;
-    unsigned long long* nfail = nullptr;
-    RG_TRY(dalloc(&fails, (size_t)n, s));
-    int st = dalloc(&nfail, 1, s);
-    if (st == RG_OK) {
-        cudaMemsetAsync(nfail, 0, sizeof(unsigned long long), s);
+    const int64_t nb = 2 * (nx - 1) + 2 * (ny - 1);
+    int64_t nbins64 = nb / 2;
+    if (nbins64 < 1) nbins64 = 1;
+    if (nbins64 > (1 << 16)) nbins64 = 1 << 16;
+    const int nbins = (int)nbins64;
+    const int64_t cap = 8 * nb + 2 * nbins64;
+    int64_t *fails = nullptr, *hard = nullptr, *ptr = nullptr, *total = nullptr;
+    unsigned long long* nfail = nullptr;  // [0] walk failures, [1] points for the exhaustive scan
+    unsigned *counts = nullptr, *overflow = nullptr;
+    int32_t* items = nullptr;
+    YBins* bp = nullptr;
+    int st = RG_OK;
+    do {
+        if ((st = dalloc(&fails, (size_t)n, s))) break;
+        if ((st = dalloc(&hard, (size_t)n, s))) break;
+        if ((st = dalloc(&nfail, 2, s))) break;
+        if ((st = dalloc(&counts, (size_t)nbins + 1, s))) break;
+        if ((st = dalloc(&overflow, 1, s))) break;
+        if ((st = dalloc(&ptr, (size_t)nbins + 1, s))) break;
+        if ((st = dalloc(&total, 1, s))) break;
+        if ((st = dalloc(&items, (size_t)cap, s))) break;
+        if ((st = dalloc(&bp, 1, s))) break;
+        cudaMemsetAsync(nfail, 0, 2 * sizeof(unsigned long long), s);
+        cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbins + 1), s);
+        cudaMemsetAsync(overflow, 0, sizeof(unsigned), s);
         G2 g{x, y, nx, ny};
+        const unsigned eb = grid_for(nb, 128) > 1024 ? 1024 : grid_for(nb, 128);
+        ybins_params<<<1, 256, 0, s>>>(g, nb, nbins, bp);
+        ybins_fill<0><<<eb, 128, 0, s>>>(g, nb, bp, counts, nullptr, nullptr, cap, overflow);
+        if ((st = exclusive_scan_u32_to_i64(counts, ptr, nbins + 1, total, s))) break;
+        cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbins + 1), s);
+        ybins_fill<1><<<eb, 128, 0, s>>>(g, nb, bp, counts, ptr, items, cap, overflow);
         locate_walk_kernel<<<grid_for(n, 128), 128, 0, s>>>(g, px, py, n, oi, oj, fails, nfail);
-        locate_fallback_kernel<<<1024, 128, 0, s>>>(g, px, py, fails, nfail, oi, oj);
+        locate_resolve_kernel<<<1024, 128, 0, s>>>(g, nb, px, py, fails, nfail, bp, ptr, items, total, overflow,
+                                                   cap, hard, nfail + 1, oi, oj);
+        locate_exhaustive_kernel<<<1024, 128, 0, s>>>(g, px, py, hard, nfail + 1, oi, oj);
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {
             set_error("locate_2d_walk: %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
         }
-    }
+    } while (0);
     dfree(fails, s);
+    dfree(hard, s);
     dfree(nfail, s);
+    dfree(counts, s);
+    dfree(overflow, s);
+    dfree(ptr, s);
+    dfree(total, s);
+    dfree(items, s);
+    dfree(bp, s);
     return st;
 }
 

@@ -256,6 +256,43 @@ def test_locate_against_oracle(rg):
     assert_same(got[1], exp[1])
 
 
+@pytest.mark.parametrize("grid", ["rect", "wavy", "rotated"])
+def test_locate_outside_points_against_oracle(rg, grid):
+    """Points the walk cannot place: outside the grid (in concave pockets of
+    the boundary, at exactly the y of boundary vertices, at the extreme y)
+    and on the boundary itself, against the oracle's exhaustive locate."""
+    from regridding_gb300 import workloads
+
+    n = 41
+    if grid == "rect":
+        g = workloads.rect_grid(n, -1.0, 1.0)
+    elif grid == "wavy":
+        a = np.linspace(-1, 1, n)
+        x, y = np.meshgrid(a, a, indexing="ij")
+        g = (x + 0.08 * np.sin(3 * np.pi * y), y + 0.08 * np.sin(3 * np.pi * x))  # concave boundary, no folds
+    else:
+        g = workloads.distorted_grid(n, 0.4, 0.03)
+    bx = np.concatenate([g[0][:, 0], g[0][-1, :], g[0][::-1, -1], g[0][0, ::-1]])
+    by = np.concatenate([g[1][:, 0], g[1][-1, :], g[1][::-1, -1], g[1][0, ::-1]])
+    rng = np.random.default_rng(11)
+    pts = [
+        (bx, by),  # boundary vertices
+        (0.5 * (bx[:-1] + bx[1:]), 0.5 * (by[:-1] + by[1:])),  # boundary edge midpoints
+        (rng.uniform(-1.6, 1.6, bx.size), by),  # the y of every boundary vertex
+        (rng.uniform(-1.6, 1.6, 64), np.full(64, by.min())),
+        (rng.uniform(-1.6, 1.6, 64), np.full(64, by.max())),
+        (rng.uniform(-1.6, 1.6, 3000), rng.uniform(-1.6, 1.6, 3000)),
+        (np.array([5.0, -5.0, 0.0, 0.0]), np.array([0.0, 0.0, 5.0, -5.0])),
+    ]
+    px = np.concatenate([p[0] for p in pts])
+    py = np.concatenate([p[1] for p in pts])
+    exp = oracle.locate(g, px, py, "brute")
+    got = rg.locate_2d(g, px, py, method="brute")
+    assert_same(got[0], exp[0])
+    assert_same(got[1], exp[1])
+    assert np.sum(exp[0] == np.iinfo(np.int64).max) > 100  # many outside points exercised
+
+
 def test_find_indices_2d_extension(rg):
     c = CURVI.case("curvi33")
     gi, go = c.tuple("ci"), c.tuple("co")

@@ -234,6 +234,24 @@ int rg_transpose_conservative_scale(const int64_t* d_in, const int64_t* d_out, c
                                     const double* d_vol_out, int64_t n_out, const double* d_w_in,
                                     double* d_result, rg_stream_t stream);
 
+/* Gradient of sum_{d,o} grad_out[d, o] * (W values)[d, o] with respect to the
+ * output-grid vertex coordinates, for conservative 2D weights w built from
+ * the given grids (the backward pass of a differentiable regrid; d_values and
+ * d_grad_out are (stack, n_in) and (stack, n_out) of dtype RG_F32/RG_F64).
+ * Writes d_grad_xo/d_grad_yo (nxo x nyo, zeroed first).  The derivative of
+ * each overlap area comes from the overlap polygon of the output quad clipped
+ * by the input quad, so input cells must be convex (RG_ERR_UNSUPPORTED
+ * otherwise).  d_w_check, when not NULL, receives the weight of every stored
+ * entry (CSR order) recomputed from that polygon.  Synchronises `stream`.
+ * No upstream counterpart: the upstream weights have no derivative; this is
+ * the adjoint of the overlap areas of
+ * regridding/_weights/_weights_conservative_2d/_weights_conservative_2d.py:752-830. */
+int rg_conservative_2d_grad_output(rg_weights w, const double* d_xi, const double* d_yi, int64_t nxi,
+                                   int64_t nyi, const double* d_xo, const double* d_yo, int64_t nxo,
+                                   int64_t nyo, const double* d_w_in, const void* d_values,
+                                   const void* d_grad_out, int dtype, int64_t stack, double* d_grad_xo,
+                                   double* d_grad_yo, double* d_w_check, rg_stream_t stream);
+
 /* Device bytes currently held by a handle: the CSR plus whatever state
  * applies have made on first use (float32 weights, tile lists, transposed
  * CSR).  Used by caches that account weights against an HBM budget.  No

@@ -51,6 +51,7 @@ SIGNATURES = {
     "rg_conservative_1d": [_P, _I, _I, _P, _I, _I, _I, _P, _I, _I, _P, _P, _P, _P, _P],
     "rg_transpose_conservative_scale": [_P, _P, _P, _I, _P, _I, _P, _I, _P, _P, _P],
     "rg_weights_device_bytes": [_P, ctypes.POINTER(_I)],
+    "rg_conservative_2d_grad_output": [_P, _P, _P, _I, _I, _P, _P, _I, _I, _P, _P, _P, _C, _I, _P, _P, _P, _P],
     "rg_hash64": [_P, _I, ctypes.c_uint64, ctypes.POINTER(ctypes.c_uint64)],
 }
 

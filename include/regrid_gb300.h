@@ -107,6 +107,18 @@ int rg_weights_set_output_shape(rg_weights w, int64_t n0, int64_t n1);
 int rg_weights_export_coo(rg_weights w, int64_t* d_in, int64_t* d_out, double* d_val,
                           rg_stream_t stream);
 
+/* Record the 2D shape of the input cells (columns of the matrix), which
+ * lets the fast float32 apply stage input boxes with tensor-map copies.
+ * Optional (weights built by rg_build_conservative_2d have it); fixed once a
+ * fast float32 apply has run (RG_ERR_ARG). */
+int rg_weights_set_input_shape(rg_weights w, int64_t n0, int64_t n1);
+
+/* Synchronise `stream` and report a failure that an earlier asynchronous
+ * apply with this handle recorded on the device: a staged copy that did not
+ * complete within its bounded wait (RG_ERR_CUDA; the results of that apply
+ * are invalid).  RG_OK when there was none. */
+int rg_weights_check(rg_weights w, rg_stream_t stream);
+
 /* Free a handle (stream ordered on `stream`). */
 int rg_weights_free(rg_weights w, rg_stream_t stream);
 

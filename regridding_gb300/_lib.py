@@ -39,6 +39,8 @@ SIGNATURES = {
     "rg_weights_set_output_shape": [_P, _I, _I],
     "rg_weights_export_coo": [_P, _P, _P, _P, _P],
     "rg_weights_free": [_P, _P],
+    "rg_weights_set_input_shape": [_P, _I, _I],
+    "rg_weights_check": [_P, _P],
     "rg_apply": [_P, _P, _C, _P, _C, _I, _C, _P],
     "rg_apply_transpose": [_P, _P, _C, _P, _C, _I, _C, _P],
     "rg_apply_host": [_P, _P, _C, _P, _C, _I, _C, _I, _P],

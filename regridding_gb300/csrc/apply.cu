@@ -164,6 +164,10 @@ int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, con
 
 int tiled_lists_for(rg_weights_s* W, const float* vin, cudaStream_t s, int* g, bool* made);
 int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack);
+int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made);
+int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int ensure_transposed(rg_weights_s* W, cudaStream_t s);
 
 // Every apply goes through here.  The per-handle state an apply needs beyond
@@ -177,11 +181,13 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
     RG_CHECK(dtype_out == RG_F32 || dtype_out == RG_F64, RG_ERR_ARG, "apply: bad output dtype");
     RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST, RG_ERR_ARG, "apply: bad accumulation mode");
     if (stack <= 0) return RG_OK;
-    // the bandwidth path: float32 in and out, gather lists staged in shared memory
+    // the bandwidth path: float32 in and out, input staged in shared memory (by
+    // tensor-map copies when the input grid shape allows, else by the warps)
     const bool tiled = !transposed && acc == RG_ACC_FAST && dtype_in == RG_F32 && dtype_out == RG_F32 &&
                        W->n_out > 0 && W->nnz > 0;
     const bool need32 = acc == RG_ACC_FAST && dtype_out == RG_F32 && W->nnz > 0;
     int g = 0;
+    bool use_box = false;
     {
         std::lock_guard<std::mutex> lock(W->mu);
         bool made = false;
@@ -196,7 +202,27 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
                 transposed ? W->t_val : W->val, *v32, W->nnz);
             made = true;
         }
-        if (tiled) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
+        if (tiled && box_usable(W, (const float*)vin, stack)) {
+            RG_TRY(box_lists_for(W, s, &made));
+            use_box = W->box_state == 1;
+            if (use_box && W->box_cfg == -1) {
+                if (made) RG_CUDA(cudaStreamSynchronize(s));
+                made = false;
+                RG_TRY(tune_box(W, (const float*)vin, (float*)vout, stack, s));
+            }
+            use_box = use_box && W->box_cfg >= 0;
+        }
+        if (tiled && !use_box) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
+        if (made) RG_CUDA(cudaStreamSynchronize(s));
+    }
+    if (use_box) {
+        const int st = apply_box(W, (const float*)vin, (float*)vout, stack, s);
+        if (st != RG_ERR_UNSUPPORTED) return st;
+        // the tuned configuration does not take this call (fewer slices than
+        // a stage): the warp-staged kernel does, with its own lists
+        std::lock_guard<std::mutex> lock(W->mu);
+        bool made = false;
+        RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
         if (made) RG_CUDA(cudaStreamSynchronize(s));
     }
     if (tiled) return apply_tiled(W, g, (const float*)vin, (float*)vout, stack, s);

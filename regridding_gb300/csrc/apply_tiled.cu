@@ -14,6 +14,13 @@
 // shared-memory stage interleaved by slice; each entry of a lane's row is
 // then one 128-bit shared load that serves all 4 slices.  A second, scalar variant handles
 // inputs whose slices are not 16-byte aligned.
+#include <cuda.h>  // CUtensorMap and its enums; the encoder comes from the runtime's driver entry point
+
+#include <algorithm>
+#include <climits>
+#include <cstdio>
+#include <cstdlib>
+
 #include "common.cuh"
 
 namespace rg {
@@ -274,6 +281,280 @@ __global__ void __launch_bounds__(32 * WARPS)
     }
 }
 
+// ---------------------------------------------------------------------------
+// TMA variant.  A block of 8 warps owns a 16 x 16 patch of output cells
+// (4 x 2 warp tiles of 4 x 8).  The input footprint of every patch lies in a
+// box of box_rows x 32 input cells (the same box size for all patches, the
+// origin per patch, its column a multiple of 4 so that a copy starts on a
+// 16-byte boundary).  A ring of NST stages, each holding SPS slices of the
+// patch's box, is filled by one 3D tensor copy per stage (columns x rows x
+// slices) issued by thread 0 and completed by the stage's "full" mbarrier
+// transaction count; every warp arrives on the stage's "empty" mbarrier when
+// it has read the stage, and thread 0 waits for all 8 before refilling it.
+// The copies run on the TMA unit, so the load/store pipe only carries the
+// gathers of the reduction (one 32-bit shared load per entry and slice).
+// Box rows are 128 bytes and written with the 128-byte swizzle (16-byte
+// chunk c of row r lands at chunk c ^ (r & 7) of that row), which spreads
+// the gathers of vertically neighbouring cells over different banks; the
+// entries' slots carry the swizzle.  Waits are bounded: a copy that does not
+// land sets FLAG_TIMEOUT and the block leaves after a bounded drain.
+// ---------------------------------------------------------------------------
+
+constexpr int PATCH = 16;      // output cells per patch side
+constexpr int PATCH_WARPS = 8; // 4 x 2 warp tiles of 4 x 8
+constexpr int PBOX_C = 32;     // box columns: one 128-byte swizzle span
+constexpr int PBOX_MAX_R = 32; // box rows at most
+constexpr int PBOX_MIN_SPS = 2;
+
+__device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];\n" ::"r"(smem_u32(bar)) : "memory");
+}
+// try_wait with a suspend-time hint (ns): the thread sleeps instead of spinning
+__device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
+    unsigned ok;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2, %3;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity), "r"(20000u)
+        : "memory");
+    return ok != 0;
+}
+// bounded wait: gives up after 2^16 polls (each suspends at most ~20 us)
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+    for (int it = 0; it < (1 << 16); it++)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+__device__ __forceinline__ void tma_load_3d(float* dst, const CUtensorMap* map, int x, int y, int z, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, %4}], "
+        "[%5];\n" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(z), "r"(smem_u32(bar))
+        : "memory");
+}
+
+struct PatchGrid {
+    int64_t n0, n1;     // output cells
+    int64_t patches1;   // patches along axis 1
+};
+
+__device__ __forceinline__ int64_t patch_cell(const PatchGrid& P, int64_t p, int r, int c) {
+    const int64_t pi = p / P.patches1, pj = p - pi * P.patches1;
+    const int64_t i = pi * PATCH + r, j = pj * PATCH + c;
+    return (i < P.n0 && j < P.n1) ? i * P.n1 + j : -1;
+}
+
+// One block of 256 threads per patch, a thread per output cell.  PASS 0:
+// footprint (origin, extent) of every patch; PASS 1: patches that fit the
+// box get their entries' swizzled slots, the others are marked for direct
+// gathers (origin row -2).
+template <int PASS>
+__global__ void __launch_bounds__(256)
+    prepare_patch(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, PatchGrid P, int64_t n1_in,
+                  int2* __restrict__ origin, int2* __restrict__ extent, unsigned* __restrict__ stats, int BR,
+                  uint16_t* __restrict__ slot) {
+    __shared__ int red[4][8];
+    const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+    const int64_t p = blockIdx.x;
+    const int64_t o = patch_cell(P, p, t / PATCH, t % PATCH);
+    int64_t s = 0, e = 0;
+    if (o >= 0) {
+        s = row_ptr[o];
+        e = row_ptr[o + 1];
+    }
+    if (PASS == 0) {
+        int rmin = INT_MAX, rmax = -1, cmin = INT_MAX, cmax = -1;
+        for (int64_t k = s; k < e; k++) {
+            const int c = col[k];
+            const int r = (int)(c / n1_in), cc = (int)(c - (int64_t)r * n1_in);
+            rmin = min(rmin, r);
+            rmax = max(rmax, r);
+            cmin = min(cmin, cc);
+            cmax = max(cmax, cc);
+        }
+        rmin = __reduce_min_sync(0xffffffffu, rmin);
+        cmin = __reduce_min_sync(0xffffffffu, cmin);
+        rmax = __reduce_max_sync(0xffffffffu, rmax);
+        cmax = __reduce_max_sync(0xffffffffu, cmax);
+        if (lane == 0) {
+            red[0][warp] = rmin;
+            red[1][warp] = cmin;
+            red[2][warp] = rmax;
+            red[3][warp] = cmax;
+        }
+        __syncthreads();
+        if (t == 0) {
+            for (int w = 1; w < 8; w++) {
+                rmin = min(rmin, red[0][w]);
+                cmin = min(cmin, red[1][w]);
+                rmax = max(rmax, red[2][w]);
+                cmax = max(cmax, red[3][w]);
+            }
+            if (rmax < 0) {
+                origin[p] = make_int2(-1, -1);
+                extent[p] = make_int2(0, 0);
+            } else {
+                const int c0 = cmin & ~3;
+                origin[p] = make_int2(rmin, c0);
+                extent[p] = make_int2(rmax - rmin + 1, cmax - c0 + 1);
+                atomicMax(&stats[0], (unsigned)(rmax - rmin + 1));
+                atomicMax(&stats[1], (unsigned)(cmax - c0 + 1));
+            }
+        }
+        return;
+    }
+    const int2 org = origin[p];
+    const int2 ext = extent[p];
+    if (org.x < 0) return;
+    if (ext.x > BR || ext.y > PBOX_C) {
+        __syncthreads();  // every thread has read origin before it changes
+        if (t == 0) {
+            origin[p] = make_int2(-2, -2);
+            atomicAdd(&stats[2], 1u);
+        }
+        return;
+    }
+    for (int64_t k = s; k < e; k++) {
+        const int c = col[k];
+        const int r = (int)(c / n1_in) - org.x, cc = (int)(c - (int64_t)(c / n1_in) * n1_in) - org.y;
+        slot[k] = (uint16_t)(r * PBOX_C + ((((cc >> 2) ^ (r & 7)) << 2) | (cc & 3)));
+    }
+}
+
+template <int SPS, int NST, int MINB>
+__global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
+    apply_patch_tma(const __grid_constant__ CUtensorMap tmap, const int64_t* __restrict__ row_ptr,
+                    const int32_t* __restrict__ col, const uint16_t* __restrict__ slot, const float* __restrict__ val,
+                    PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
+                    unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
+                    int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags) {
+    __shared__ __align__(8) uint64_t full[NST], empty[NST];
+    extern __shared__ __align__(1024) float ring[];
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int64_t p = blockIdx.x;
+    const int64_t o = patch_cell(P, p, 4 * (warp >> 1) + (lane >> 3), 8 * (warp & 1) + (lane & 7));
+    const int64_t d0 = (int64_t)blockIdx.y * chunk;
+    const int64_t d1 = d0 + chunk < stack ? d0 + chunk : stack;
+    int64_t s = 0, e = 0;
+    if (o >= 0) {
+        s = row_ptr[o];
+        e = row_ptr[o + 1];
+    }
+    const int nk = (int)(e - s);
+    float* out = vout + (o >= 0 ? o : 0);
+    const int2 org = origin[p];
+    if (org.x < 0) {
+        // no entries (all zeros) or a footprint larger than the box: the whole block
+        if (o >= 0) apply_direct(s, e, col, val, vin, n_in, out, n_out, d0, d1);
+        return;
+    }
+    const int plane = BR * PBOX_C;
+    // rows of slice q start at row q * BR of the swizzle pattern: with BR a
+    // multiple of 4, odd slices see the pattern shifted by 4 rows, which is
+    // the chunk index xor 4 (slot xor 16)
+    const int flip = (BR & 4) ? 16 : 0;
+    int li[CACHED_T];
+    float w[CACHED_T];
+#pragma unroll
+    for (int k = 0; k < CACHED_T; k++) {
+        li[k] = k < nk ? (int)slot[s + k] : 0;
+        w[k] = k < nk ? val[s + k] : 0.f;
+    }
+    if (t == 0) {
+        for (int k = 0; k < NST; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], PATCH_WARPS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    const int64_t ngroups = (d1 - d0 + SPS - 1) / SPS;
+    auto issue = [&](int st, int64_t grp) {
+        mbar_expect_tx(&full[st], stage_bytes);
+        tma_load_3d(ring + (int64_t)st * stage_floats, &tmap, org.y, org.x, (int)(d0 + grp * SPS), &full[st]);
+    };
+    if (t == 0)
+        for (int k = 0; k < NST && k < ngroups; k++) issue(k, k);
+    for (int64_t grp = 0; grp < ngroups; grp++) {
+        const int st = (int)(grp % NST);
+        const unsigned ph = (unsigned)((grp / NST) & 1);
+        const bool got = mbar_wait_bounded(&full[st], ph);
+        if (!__all_sync(0xffffffffu, got)) {
+            if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
+            if (t == 0)  // the copies still in flight: bounded wait before leaving
+                for (int64_t q = grp + 1; q < grp + NST && q < ngroups; q++)
+                    (void)mbar_wait_bounded(&full[q % NST], (unsigned)((q / NST) & 1));
+            return;
+        }
+        const float* buf = ring + (int64_t)st * stage_floats;
+        const int64_t ds = d0 + grp * SPS;
+        if (o >= 0) {
+            float acc[SPS];
+#pragma unroll
+            for (int q = 0; q < SPS; q++) acc[q] = 0.f;
+#pragma unroll
+            for (int k = 0; k < CACHED_T; k++) {
+                if (k < nk) {
+#pragma unroll
+                    for (int q = 0; q < SPS; q++)
+                        acc[q] = fmaf(w[k], buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))], acc[q]);
+                }
+            }
+            for (int64_t k = s + CACHED_T; k < e; k++) {
+                const float wk = val[k];
+                const int sk = slot[k];
+#pragma unroll
+                for (int q = 0; q < SPS; q++) acc[q] = fmaf(wk, buf[q * plane + (sk ^ ((q & 1) ? flip : 0))], acc[q]);
+            }
+#pragma unroll
+            for (int q = 0; q < SPS; q++)
+                if (ds + q < d1) out[(ds + q) * n_out] = acc[q];
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);  // this warp is done with the stage
+        if (t == 0 && grp + NST < ngroups) {
+            if (!mbar_wait_bounded(&empty[st], ph)) {
+                atomicOr(flags, FLAG_TIMEOUT);
+                for (int64_t q = grp + 1; q < grp + NST && q < ngroups; q++)
+                    (void)mbar_wait_bounded(&full[q % NST], (unsigned)((q / NST) & 1));
+                return;
+            }
+            // the warps' generic-proxy reads of the stage before the async-proxy writes
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            issue(st, grp + NST);
+        }
+    }
+}
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                  const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_tiled() {
+    static std::once_flag once;
+    static EncodeTiledFn fn = nullptr;
+    std::call_once(once, []() {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+        cudaGetLastError();
+    });
+    return fn;
+}
+
 // Scalar variant (slices not 16-byte aligned): single cells, PER per lane.
 template <int PER>
 __global__ void __launch_bounds__(32 * WARPS)
@@ -494,6 +775,221 @@ int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int
 #undef RG_ARGS
     RG_CUDA(cudaGetLastError());
     return RG_OK;
+}
+
+// Whether the TMA apply can take this call: output and input grid shapes
+// known, input rows of whole 16-byte chunks, 16-byte aligned slices, and a
+// stack of at least the smallest stage.
+bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack) {
+    return W->box_state >= 0 && W->box_cfg != -2 && W->out_shape0 > 0 && W->out_shape1 > 0 &&
+           W->out_shape0 * W->out_shape1 == W->n_out && W->in_shape0 > 0 && W->in_shape1 > 0 &&
+           W->in_shape1 % 4 == 0 && W->in_shape0 * W->in_shape1 == W->n_in && ((uintptr_t)vin & 15) == 0 &&
+           stack >= PBOX_MIN_SPS && W->n_in < INT32_MAX && stack < INT32_MAX && encode_tiled() != nullptr;
+}
+
+PatchGrid patch_grid(const rg_weights_s* W) {
+    PatchGrid P;
+    P.n0 = W->out_shape0;
+    P.n1 = W->out_shape1;
+    P.patches1 = (P.n1 + PATCH - 1) / PATCH;
+    return P;
+}
+
+// Build the patch lists of W (the caller holds the handle's lock; *made set
+// when anything was launched).  Leaves box_state -1 when the footprints do
+// not fit a box (more than 1 % of the patches, and more than 4, would need
+// direct gathers).
+int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
+    if (W->box_state != 0) return RG_OK;
+    *made = true;
+    const PatchGrid P = patch_grid(W);
+    const int64_t patches = ((P.n0 + PATCH - 1) / PATCH) * P.patches1;
+    RG_CHECK(patches < 0x7fffffff, RG_ERR_UNSUPPORTED, "apply: too many output patches");
+    int2* extent = nullptr;
+    unsigned* stats = nullptr;
+    int st = RG_OK;
+    do {
+        if ((st = dalloc(&W->box_origin, (size_t)patches, s))) break;
+        if ((st = dalloc(&extent, (size_t)patches, s))) break;
+        if ((st = dalloc(&stats, 4, s))) break;
+        if ((st = dalloc(&W->box_slot, (size_t)W->nnz, s))) break;
+        if (W->dflags == nullptr) {
+            if ((st = dalloc(&W->dflags, 1, s))) break;
+            cudaMemsetAsync(W->dflags, 0, sizeof(unsigned), s);
+        }
+        cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned), s);
+        prepare_patch<0><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, W->in_shape1, W->box_origin,
+                                                           extent, stats, 0, nullptr);
+        unsigned h[4] = {0, 0, 0, 0};
+        cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("apply (patch lists): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        // box rows: a multiple of 4 (keeps the swizzle phase of every slice at 0 or 4)
+        const int BR = (int)((std::min<unsigned>(std::max<unsigned>(h[0], 1u), PBOX_MAX_R) + 3) & ~3u);
+        prepare_patch<1><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, W->in_shape1, W->box_origin,
+                                                           extent, stats, BR, W->box_slot);
+        cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("apply (patch lists): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        W->box_rows = BR;
+        W->box_cols = PBOX_C;
+        W->box_patches = patches;
+        const bool few = (int64_t)h[2] * 100 <= patches || h[2] <= 4;  // patches left to direct gathers
+        W->box_state = few && BR <= W->in_shape0 && PBOX_C <= W->in_shape1 ? 1 : -1;
+    } while (0);
+    dfree(extent, s);
+    dfree(stats, s);
+    if (st != RG_OK || W->box_state != 1) {
+        dfree(W->box_origin, s);
+        dfree(W->box_slot, s);
+        W->box_origin = nullptr;
+        W->box_slot = nullptr;
+        if (st == RG_OK) W->box_state = -1;
+    }
+    return st;
+}
+
+// Configurations of the TMA apply: slices per stage, stages, and the blocks
+// per SM its registers are capped for (0: no cap).  The autotuner below
+// times each on the first apply of a handle; RG_APPLY_BOX_CONFIG="sps,nst,minb"
+// forces one.
+struct BoxConfig {
+    int sps, nst, minb;
+};
+constexpr BoxConfig kBoxConfigs[] = {{4, 2, 0}, {4, 2, 4}, {4, 3, 4}, {2, 3, 4}, {2, 4, 4}, {8, 2, 0}, {4, 3, 0}};
+constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]));
+
+template <int SPS, int NST, int MINB>
+int launch_patch(const rg_weights_s* W, const CUtensorMap& map, const float* vin, float* vout, int64_t stack,
+                 cudaStream_t s) {
+    const int BR = W->box_rows;
+    const int stage_floats = (SPS * BR * PBOX_C + 255) & ~255;  // stages start on 1024-byte boundaries
+    const unsigned stage_bytes = (unsigned)(SPS * BR * PBOX_C * 4);
+    const size_t smem = (size_t)NST * stage_floats * sizeof(float);
+    if (smem > 200 * 1024) return RG_ERR_UNSUPPORTED;
+    static std::once_flag attr;
+    std::call_once(attr, []() {
+        cudaFuncSetAttribute(apply_patch_tma<SPS, NST, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             200 * 1024);
+        cudaGetLastError();
+    });
+    const int64_t patches = W->box_patches;
+    // split the stack over gridDim.y only when the patches alone give less
+    // than ~4 waves of 4 blocks per SM on 152 SMs
+    const int64_t target_blocks = 152 * 4 * 4;
+    int64_t chunks = (target_blocks + patches - 1) / patches;
+    if (chunks < 1) chunks = 1;
+    int64_t chunk = (stack + chunks - 1) / chunks;
+    chunk = (chunk + SPS - 1) / SPS * SPS;
+    if ((stack + chunk - 1) / chunk > 65535) chunk = ((stack + 65534) / 65535 + SPS - 1) / SPS * SPS;
+    const int64_t nchunks = (stack + chunk - 1) / chunk;
+    dim3 grid((unsigned)patches, (unsigned)nchunks);
+    apply_patch_tma<SPS, NST, MINB><<<grid, 32 * PATCH_WARPS, smem, s>>>(
+        map, W->row_ptr, W->col, W->box_slot, W->val32, patch_grid(W), patches, W->box_origin, BR, stage_floats,
+        stage_bytes, vin, W->n_in, vout, W->n_out, stack, chunk, W->dflags);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+    const BoxConfig c = kBoxConfigs[cfg];
+    if (stack < c.sps) return RG_ERR_UNSUPPORTED;
+    CUtensorMap map;
+    const cuuint64_t dims[3] = {(cuuint64_t)W->in_shape1, (cuuint64_t)W->in_shape0, (cuuint64_t)stack};
+    const cuuint64_t strides[2] = {(cuuint64_t)W->in_shape1 * 4, (cuuint64_t)W->n_in * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)PBOX_C, (cuuint32_t)W->box_rows, (cuuint32_t)c.sps};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    CUresult r = encode_tiled()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)vin, dims, strides, box, estr,
+                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+    if (r != CUDA_SUCCESS) return RG_ERR_UNSUPPORTED;
+    switch (cfg) {
+        case 0: return launch_patch<4, 2, 0>(W, map, vin, vout, stack, s);
+        case 1: return launch_patch<4, 2, 4>(W, map, vin, vout, stack, s);
+        case 2: return launch_patch<4, 3, 4>(W, map, vin, vout, stack, s);
+        case 3: return launch_patch<2, 3, 4>(W, map, vin, vout, stack, s);
+        case 4: return launch_patch<2, 4, 4>(W, map, vin, vout, stack, s);
+        case 5: return launch_patch<8, 2, 0>(W, map, vin, vout, stack, s);
+        case 6: return launch_patch<4, 3, 0>(W, map, vin, vout, stack, s);
+    }
+    return RG_ERR_UNSUPPORTED;
+}
+
+int forced_box_config() {
+    const char* env = getenv("RG_APPLY_BOX_CONFIG");
+    if (!env) return -1;
+    int a = 0, b = 0, c = 0;
+    if (sscanf(env, "%d,%d,%d", &a, &b, &c) != 3) return -1;
+    for (int k = 0; k < kNumBoxConfigs; k++)
+        if (kBoxConfigs[k].sps == a && kBoxConfigs[k].nst == b && kBoxConfigs[k].minb == c) return k;
+    return -1;
+}
+
+// Autotuner: on the first TMA apply of a handle, time every configuration
+// on the real call (each run writes the same result) and keep the fastest.
+// The caller holds the handle's lock; synchronises the stream.
+int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+    if (W->box_cfg >= 0) return RG_OK;
+    const int forced = forced_box_config();
+    if (forced >= 0) {
+        W->box_cfg = forced;
+        return RG_OK;
+    }
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    RG_CUDA(cudaEventCreate(&e0));
+    if (cudaEventCreate(&e1) != cudaSuccess) {
+        cudaEventDestroy(e0);
+        cudaGetLastError();
+        return RG_ERR_CUDA;
+    }
+    int best = -1;
+    float best_ms = 0;
+    int st = RG_OK;
+    for (int k = 0; k < kNumBoxConfigs && st == RG_OK; k++) {
+        if (launch_box_config(W, k, vin, vout, stack, s) != RG_OK) {  // warm-up; skips configs that do not fit
+            cudaGetLastError();
+            continue;
+        }
+        float ms = 0;
+        for (int rep = 0; rep < 2; rep++) {
+            cudaEventRecord(e0, s);
+            launch_box_config(W, k, vin, vout, stack, s);
+            cudaEventRecord(e1, s);
+            if (cudaEventSynchronize(e1) != cudaSuccess) {
+                set_error("apply (tuning): %s", cudaGetErrorString(cudaGetLastError()));
+                st = RG_ERR_CUDA;
+                break;
+            }
+            float tm = 0;
+            cudaEventElapsedTime(&tm, e0, e1);
+            ms = rep == 0 ? tm : std::min(ms, tm);
+        }
+        if (st == RG_OK && (best < 0 || ms < best_ms)) {
+            best = k;
+            best_ms = ms;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (st != RG_OK) return st;
+    W->box_cfg = best >= 0 ? best : -2;
+    return RG_OK;
+}
+
+// Launch the TMA apply; returns RG_ERR_UNSUPPORTED (nothing launched) when
+// the tuned configuration does not take this call, so the caller can take
+// another kernel.
+int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+    if (W->box_cfg < 0) return RG_ERR_UNSUPPORTED;
+    return launch_box_config(W, W->box_cfg, vin, vout, stack, s);
 }
 
 }  // namespace rg

@@ -153,6 +153,9 @@ void free_weights(rg_weights_s* W, cudaStream_t s) {
         dfree(W->t_gidx[g], s);
         dfree(W->t_slot[g], s);
     }
+    dfree(W->box_origin, s);
+    dfree(W->box_slot, s);
+    dfree(W->dflags, s);
     delete W;
 }
 
@@ -343,6 +346,33 @@ int rg_weights_export_coo(rg_weights w, int64_t* d_in, int64_t* d_out, double* d
     return RG_OK;
 }
 
+int rg_weights_set_input_shape(rg_weights w, int64_t n0, int64_t n1) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_weights_set_input_shape: NULL handle");
+    RG_CHECK(n0 * n1 == w->n_in, RG_ERR_ARG, "rg_weights_set_input_shape: %lld x %lld != %lld", (long long)n0,
+             (long long)n1, (long long)w->n_in);
+    std::lock_guard<std::mutex> lock(w->mu);
+    if (w->in_shape0 == n0 && w->in_shape1 == n1) return RG_OK;
+    RG_CHECK(w->box_state == 0, RG_ERR_ARG,
+             "rg_weights_set_input_shape: the input tiling is fixed once a fast float32 apply has run");
+    w->in_shape0 = n0;
+    w->in_shape1 = n1;
+    return RG_OK;
+}
+
+int rg_weights_check(rg_weights w, rg_stream_t stream) {
+    RG_CHECK(w, RG_ERR_ARG, "rg_weights_check: NULL handle");
+    RG_CUDA(cudaStreamSynchronize((cudaStream_t)stream));
+    unsigned fl = 0;
+    {
+        std::lock_guard<std::mutex> lock(w->mu);
+        if (!w->dflags) return RG_OK;
+        RG_CUDA(cudaMemcpy(&fl, w->dflags, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    }
+    RG_CHECK(!(fl & FLAG_TIMEOUT), RG_ERR_CUDA,
+             "an earlier apply with this handle gave up waiting for its staged copies (its results are invalid)");
+    return RG_OK;
+}
+
 int rg_weights_free(rg_weights w, rg_stream_t stream) {
     if (w) free_weights(w, (cudaStream_t)stream);
     return RG_OK;
@@ -430,6 +460,7 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes) {
     if (w->t_val32) b += nnz * 4;
     for (int g = 0; g < 2; g++)
         if (w->tiled_ready[g]) b += (w->t_tiles + 1) * 8 + nnz * 2;  // list pointers + slots (lists are small)
+    if (w->box_state == 1) b += w->box_patches * 8 + nnz * 2;
     *bytes = b;
     return RG_OK;
 }

@@ -52,6 +52,7 @@ enum DeviceFlag : unsigned {
     FLAG_SEAT_OUTSIDE = 1u << 1,
     FLAG_BUCKET_TOO_LONG = 1u << 2,
     FLAG_CAPACITY = 1u << 3,
+    FLAG_TIMEOUT = 1u << 4,  // a bounded wait for an asynchronous copy gave up
 };
 
 // ---------------------------------------------------------------------------
@@ -131,8 +132,10 @@ struct rg_weights_s {
     int32_t* t_col = nullptr;
     double* t_val = nullptr;
     float* t_val32 = nullptr;
-    // (optional) output grid shape for 2D tiling of the apply
+    // (optional) output grid shape for 2D tiling of the apply, and input grid
+    // shape for the tensor-map (TMA) staging of the input slices
     int64_t out_shape0 = 0, out_shape1 = 0;
+    int64_t in_shape0 = 0, in_shape1 = 0;
     // warp-tile lists of the float32 fast apply, built on first use; index 0
     // lists single cells, index 1 lists 32-byte sectors of 8 cells
     bool tiled_ready[2] = {false, false};
@@ -141,6 +144,17 @@ struct rg_weights_s {
     int64_t* t_gptr[2] = {nullptr, nullptr};   // [tiles + 1]
     int32_t* t_gidx[2] = {nullptr, nullptr};   // the lists
     uint16_t* t_slot[2] = {nullptr, nullptr};  // [nnz] staged slot of each entry
+    // patch lists of the TMA apply: per 16 x 16 patch of output cells the
+    // origin (row, column) of a fixed box_rows x box_cols box of input cells
+    // holding its footprint (row -1: no entries, -2: footprint larger than
+    // the box), and per entry its (swizzled) offset in the box
+    int box_state = 0;  // 0 not built, 1 ready, -1 not applicable
+    int box_rows = 0, box_cols = 0;
+    int64_t box_patches = 0;
+    int box_cfg = -1;  // configuration chosen by the autotuner (-1 not tuned, -2 none fits)
+    int2* box_origin = nullptr;
+    uint16_t* box_slot = nullptr;
+    unsigned* dflags = nullptr;  // device error word of the asynchronous (TMA) apply
     int device = 0;
     std::mutex mu;  // guards the lazily made state above (made on first use by an apply)
 };

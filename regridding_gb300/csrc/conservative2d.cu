@@ -1386,6 +1386,8 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
         W->nnz = nnz;
         W->out_shape0 = ncx_out;
         W->out_shape1 = ncy_out;
+        W->in_shape0 = ncx_in;
+        W->in_shape1 = ncy_in;
     } while (0);
 
     dfree(area_in, s);

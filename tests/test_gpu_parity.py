@@ -6,6 +6,8 @@ the upstream arithmetic exactly); exact-mode applies are bit for bit; the
 float32 fast apply is checked to 1e-6 relative.
 """
 
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -519,15 +521,18 @@ def _local_coo(rng, n0_in, n1_in, n0_out, n1_out, per_row=(1, 9), empty=0.0, spr
 
 @pytest.mark.parametrize(
     "case",
-    ["vec", "vec_tail4", "scalar_odd", "unaligned", "long_lists", "huge_tile", "no_shape", "empty_rows"])
+    ["vec", "vec_tail4", "scalar_odd", "unaligned", "long_lists", "huge_tile", "no_shape", "empty_rows",
+     "tma", "tma_some_far", "tma_all_far"])
 @pytest.mark.parametrize("stack", [1, 7, 64])
 def test_fast_apply_paths(rg, case, stack):
     """Every branch of the float32 fast apply against the oracle's float64
     apply: sector lists (n_in % 8 == 0 and == 4, where the last sector's
     second half lies past the slice), cell lists (n_in % 4 != 0, unaligned
     input), tiles whose lists overflow into the direct gathers, unknown
-    output shape (row tiles) and rows without entries.  float32 accumulation
-    with FMA is checked against its forward error bound."""
+    output shape (row tiles), rows without entries, and the tensor-copy
+    staging (input shape known: boxes for all tiles, for all but a few, or
+    footprints too scattered for a box).  float32 accumulation with FMA is
+    checked against its forward error bound."""
     import torch
 
     from regridding_gb300._device import DeviceWeights
@@ -543,8 +548,16 @@ def test_fast_apply_paths(rg, case, stack):
         n0_in, n1_in = 100, 64
     if case == "empty_rows":
         kw = {"empty": 0.4}
+    if case == "tma_all_far":
+        kw = {"spread": 3}
     ii, oo, vv = _local_coo(rng, n0_in, n1_in, n0_out, n1_out, **kw)
     n_in = n0_in * n1_in
+    if case == "tma_some_far":
+        # a far-away cell in 4 rows: those tiles' footprints exceed the box
+        # and take the direct gathers; the rest are staged by tensor copies
+        key = np.unique(np.concatenate([oo * n_in + ii, np.array([5, 200, 611, 1000]) * n_in + [1913, 3, 960, 47]]))
+        oo, ii = key // n_in, key % n_in
+        vv = rng.uniform(0.1, 1.0, ii.size)
     if case == "vec_tail4":
         n_in = 1796  # n_in % 8 == 4; make sure the last cell is read
         ii = np.minimum(ii, n_in - 1)
@@ -563,6 +576,10 @@ def test_fast_apply_paths(rg, case, stack):
     n_out = n0_out * n1_out
     shape = None if case == "no_shape" else (n0_out, n1_out)
     dw = DeviceWeights.from_coo(ii, oo, vv, n_in, n_out, shape)
+    if case.startswith("tma"):
+        from regridding_gb300 import _lib
+
+        _lib.call("rg_weights_set_input_shape", dw.handle, n0_in, n1_in)
     vals = rng.uniform(0.5, 2.0, (stack, n_in)).astype(np.float32)
     if case == "unaligned":
         buf = torch.empty(stack * n_in + 1, dtype=torch.float32, device="cuda")
@@ -585,3 +602,10 @@ def test_fast_apply_paths(rg, case, stack):
     # applying twice (lists already built) gives the same bits
     again = dw.apply(d_vals, accumulate="fast").cpu().numpy()
     assert_same(again, got)
+    if stack > 1:
+        # fewer slices than the tuned stage size (the warp-staged kernel takes over)
+        one = dw.apply(d_vals[:1].contiguous(), accumulate="fast").cpu().numpy()
+        assert_same(one, got[:1])
+    from regridding_gb300 import _lib
+
+    _lib.call("rg_weights_check", dw.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))

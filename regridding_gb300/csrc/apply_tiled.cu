@@ -304,7 +304,6 @@ constexpr int PATCH = 16;      // output cells per patch side
 constexpr int PATCH_WARPS = 8; // 4 x 2 warp tiles of 4 x 8
 constexpr int PBOX_C = 32;     // box columns: one 128-byte swizzle span
 constexpr int PBOX_MAX_R = 32; // box rows at most
-constexpr int PBOX_MIN_SPS = 2;
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -431,10 +430,76 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Order of every lane's entries in the TMA kernel.  At step k each lane of
+// a warp gathers its k-th entry; two lanes whose cells fall in the same
+// shared-memory bank (slot mod 32; the per-slice swizzle phase flips every
+// lane's bank alike) are served one after the other.  One warp per warp
+// tile, laid out as in the apply kernel: for every step, lane by lane, each
+// lane takes a remaining entry whose bank no earlier lane took at this step
+// (else its first remaining entry).  Writes the reordered slots and float32
+// weights (the CSR itself, which fixes the exact paths' order, is unchanged).
+// Lanes with more than ORDER_MAX entries keep the stored order.
+constexpr int ORDER_MAX = 16;
+
+__global__ void __launch_bounds__(32 * PATCH_WARPS)
+    order_patch(const int64_t* __restrict__ row_ptr, const float* __restrict__ val32, PatchGrid P,
+                const int2* __restrict__ origin, uint16_t* __restrict__ slot, float* __restrict__ box_val) {
+    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
+    const int64_t p = blockIdx.x;
+    const int64_t o = patch_cell(P, p, 4 * (warp >> 1) + (lane >> 3), 8 * (warp & 1) + (lane & 7));
+    int64_t s = 0, e = 0;
+    if (o >= 0) {
+        s = row_ptr[o];
+        e = row_ptr[o + 1];
+    }
+    const int nk = (int)(e - s);
+    const bool boxed = origin[p].x >= 0;
+    if (!boxed) return;  // block-uniform
+    if (nk > ORDER_MAX) {
+        for (int64_t k = s; k < e; k++) box_val[k] = val32[k];
+        // keep the stored order, but the other lanes still take part below
+    }
+    uint16_t sl[ORDER_MAX];
+    float vl[ORDER_MAX];
+    const int mine = nk <= ORDER_MAX ? nk : 0;
+    for (int k = 0; k < ORDER_MAX; k++) {
+        sl[k] = k < mine ? slot[s + k] : 0;
+        vl[k] = k < mine ? val32[s + k] : 0.f;
+    }
+    unsigned left = mine == 32 ? 0xffffffffu : ((1u << mine) - 1u);  // entries not yet placed
+    int kmax = mine;
+    for (int off = 16; off > 0; off >>= 1) kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, off));
+    for (int k = 0; k < kmax; k++) {
+        unsigned used = 0;  // banks taken at this step
+        for (int l = 0; l < 32; l++) {
+            if (lane == l && left) {
+                int pick = -1;
+                for (int c = 0; c < ORDER_MAX; c++)
+                    if (((left >> c) & 1) && !((used >> (sl[c] & 31)) & 1)) {
+                        pick = c;
+                        break;
+                    }
+                if (pick < 0) pick = __ffs(left) - 1;
+                left &= ~(1u << pick);
+                used |= 1u << (sl[pick] & 31);
+                // place entry `pick` at position k: registers are indexed by
+                // loop counters only, so write it out directly
+                for (int c = 0; c < ORDER_MAX; c++)
+                    if (c == pick) {
+                        slot[s + k] = sl[c];
+                        box_val[s + k] = vl[c];
+                    }
+            }
+            used = __shfl_sync(0xffffffffu, used, l);
+        }
+    }
+}
+
 template <int SPS, int NST, int MINB>
 __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     apply_patch_tma(const __grid_constant__ CUtensorMap tmap, const int64_t* __restrict__ row_ptr,
-                    const int32_t* __restrict__ col, const uint16_t* __restrict__ slot, const float* __restrict__ val,
+                    const int32_t* __restrict__ col, const uint16_t* __restrict__ slot,
+                    const float* __restrict__ bval, const float* __restrict__ val,
                     PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
                     unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
                     int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags) {
@@ -468,7 +533,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
 #pragma unroll
     for (int k = 0; k < CACHED_T; k++) {
         li[k] = k < nk ? (int)slot[s + k] : 0;
-        w[k] = k < nk ? val[s + k] : 0.f;
+        w[k] = k < nk ? bval[s + k] : 0.f;
     }
     if (t == 0) {
         for (int k = 0; k < NST; k++) {
@@ -511,7 +576,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                 }
             }
             for (int64_t k = s + CACHED_T; k < e; k++) {
-                const float wk = val[k];
+                const float wk = bval[k];
                 const int sk = slot[k];
 #pragma unroll
                 for (int q = 0; q < SPS; q++) acc[q] = fmaf(wk, buf[q * plane + (sk ^ ((q & 1) ? flip : 0))], acc[q]);
@@ -778,13 +843,12 @@ int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int
 }
 
 // Whether the TMA apply can take this call: output and input grid shapes
-// known, input rows of whole 16-byte chunks, 16-byte aligned slices, and a
-// stack of at least the smallest stage.
+// known, input rows of whole 16-byte chunks, 16-byte aligned slices.
 bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack) {
     return W->box_state >= 0 && W->box_cfg != -2 && W->out_shape0 > 0 && W->out_shape1 > 0 &&
            W->out_shape0 * W->out_shape1 == W->n_out && W->in_shape0 > 0 && W->in_shape1 > 0 &&
            W->in_shape1 % 4 == 0 && W->in_shape0 * W->in_shape1 == W->n_in && ((uintptr_t)vin & 15) == 0 &&
-           stack >= PBOX_MIN_SPS && W->n_in < INT32_MAX && stack < INT32_MAX && encode_tiled() != nullptr;
+           stack >= 1 && W->n_in < INT32_MAX && stack < INT32_MAX && encode_tiled() != nullptr;
 }
 
 PatchGrid patch_grid(const rg_weights_s* W) {
@@ -842,6 +906,9 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         W->box_rows = BR;
         W->box_cols = PBOX_C;
         W->box_patches = patches;
+        if ((st = dalloc(&W->box_val, (size_t)W->nnz, s))) break;
+        order_patch<<<(unsigned)patches, 32 * PATCH_WARPS, 0, s>>>(W->row_ptr, W->val32, P, W->box_origin,
+                                                                   W->box_slot, W->box_val);
         const bool few = (int64_t)h[2] * 100 <= patches || h[2] <= 4;  // patches left to direct gathers
         W->box_state = few && BR <= W->in_shape0 && PBOX_C <= W->in_shape1 ? 1 : -1;
     } while (0);
@@ -850,8 +917,10 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
     if (st != RG_OK || W->box_state != 1) {
         dfree(W->box_origin, s);
         dfree(W->box_slot, s);
+        dfree(W->box_val, s);
         W->box_origin = nullptr;
         W->box_slot = nullptr;
+        W->box_val = nullptr;
         if (st == RG_OK) W->box_state = -1;
     }
     return st;
@@ -868,11 +937,11 @@ constexpr BoxConfig kBoxConfigs[] = {{4, 2, 0}, {4, 2, 4}, {4, 3, 4}, {2, 3, 4},
 constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]));
 
 template <int SPS, int NST, int MINB>
-int launch_patch(const rg_weights_s* W, const CUtensorMap& map, const float* vin, float* vout, int64_t stack,
-                 cudaStream_t s) {
+int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, const float* vin, float* vout,
+                 int64_t stack, cudaStream_t s) {
     const int BR = W->box_rows;
     const int stage_floats = (SPS * BR * PBOX_C + 255) & ~255;  // stages start on 1024-byte boundaries
-    const unsigned stage_bytes = (unsigned)(SPS * BR * PBOX_C * 4);
+    const unsigned stage_bytes = (unsigned)(box_slices * BR * PBOX_C * 4);
     const size_t smem = (size_t)NST * stage_floats * sizeof(float);
     if (smem > 200 * 1024) return RG_ERR_UNSUPPORTED;
     static std::once_flag attr;
@@ -893,32 +962,34 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, const float* vin
     const int64_t nchunks = (stack + chunk - 1) / chunk;
     dim3 grid((unsigned)patches, (unsigned)nchunks);
     apply_patch_tma<SPS, NST, MINB><<<grid, 32 * PATCH_WARPS, smem, s>>>(
-        map, W->row_ptr, W->col, W->box_slot, W->val32, patch_grid(W), patches, W->box_origin, BR, stage_floats,
-        stage_bytes, vin, W->n_in, vout, W->n_out, stack, chunk, W->dflags);
+        map, W->row_ptr, W->col, W->box_slot, W->box_val, W->val32, patch_grid(W), patches, W->box_origin, BR,
+        stage_floats, stage_bytes, vin, W->n_in, vout, W->n_out, stack, chunk, W->dflags);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
 }
 
 int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
     const BoxConfig c = kBoxConfigs[cfg];
-    if (stack < c.sps) return RG_ERR_UNSUPPORTED;
+    // a stack shorter than a stage: the box carries only its slices (the
+    // stage's other slices are never stored)
+    const int bs = (int)std::min<int64_t>(c.sps, stack);
     CUtensorMap map;
     const cuuint64_t dims[3] = {(cuuint64_t)W->in_shape1, (cuuint64_t)W->in_shape0, (cuuint64_t)stack};
     const cuuint64_t strides[2] = {(cuuint64_t)W->in_shape1 * 4, (cuuint64_t)W->n_in * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)PBOX_C, (cuuint32_t)W->box_rows, (cuuint32_t)c.sps};
+    const cuuint32_t box[3] = {(cuuint32_t)PBOX_C, (cuuint32_t)W->box_rows, (cuuint32_t)bs};
     const cuuint32_t estr[3] = {1, 1, 1};
     CUresult r = encode_tiled()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)vin, dims, strides, box, estr,
                                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
                                 CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
     if (r != CUDA_SUCCESS) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
-        case 0: return launch_patch<4, 2, 0>(W, map, vin, vout, stack, s);
-        case 1: return launch_patch<4, 2, 4>(W, map, vin, vout, stack, s);
-        case 2: return launch_patch<4, 3, 4>(W, map, vin, vout, stack, s);
-        case 3: return launch_patch<2, 3, 4>(W, map, vin, vout, stack, s);
-        case 4: return launch_patch<2, 4, 4>(W, map, vin, vout, stack, s);
-        case 5: return launch_patch<8, 2, 0>(W, map, vin, vout, stack, s);
-        case 6: return launch_patch<4, 3, 0>(W, map, vin, vout, stack, s);
+        case 0: return launch_patch<4, 2, 0>(W, map, bs, vin, vout, stack, s);
+        case 1: return launch_patch<4, 2, 4>(W, map, bs, vin, vout, stack, s);
+        case 2: return launch_patch<4, 3, 4>(W, map, bs, vin, vout, stack, s);
+        case 3: return launch_patch<2, 3, 4>(W, map, bs, vin, vout, stack, s);
+        case 4: return launch_patch<2, 4, 4>(W, map, bs, vin, vout, stack, s);
+        case 5: return launch_patch<8, 2, 0>(W, map, bs, vin, vout, stack, s);
+        case 6: return launch_patch<4, 3, 0>(W, map, bs, vin, vout, stack, s);
     }
     return RG_ERR_UNSUPPORTED;
 }

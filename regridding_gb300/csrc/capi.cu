@@ -155,6 +155,7 @@ void free_weights(rg_weights_s* W, cudaStream_t s) {
     }
     dfree(W->box_origin, s);
     dfree(W->box_slot, s);
+    dfree(W->box_val, s);
     dfree(W->dflags, s);
     delete W;
 }
@@ -460,7 +461,7 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes) {
     if (w->t_val32) b += nnz * 4;
     for (int g = 0; g < 2; g++)
         if (w->tiled_ready[g]) b += (w->t_tiles + 1) * 8 + nnz * 2;  // list pointers + slots (lists are small)
-    if (w->box_state == 1) b += w->box_patches * 8 + nnz * 2;
+    if (w->box_state == 1) b += w->box_patches * 8 + nnz * 6;
     *bytes = b;
     return RG_OK;
 }

@@ -153,7 +153,8 @@ struct rg_weights_s {
     int64_t box_patches = 0;
     int box_cfg = -1;  // configuration chosen by the autotuner (-1 not tuned, -2 none fits)
     int2* box_origin = nullptr;
-    uint16_t* box_slot = nullptr;
+    uint16_t* box_slot = nullptr;  // per entry, in the order the TMA kernel gathers them
+    float* box_val = nullptr;      // float32 weights in that order
     unsigned* dflags = nullptr;  // device error word of the asynchronous (TMA) apply
     int device = 0;
     std::mutex mu;  // guards the lazily made state above (made on first use by an apply)

@@ -80,6 +80,31 @@ int rg_build_conservative_2d(const double* d_xi, const double* d_yi, int64_t nxi
                              const double* d_xo, const double* d_yo, int64_t nxo, int64_t nyo,
                              const double* d_w_in, rg_stream_t stream, rg_weights* out);
 
+/* Sweep segments per chunk of the parallel walk in conservative builds
+ * (process-wide; default 32; 0 walks whole lines in one thread each).  The
+ * RG_SWEEP_CHUNK environment variable overrides it.  Results do not depend on
+ * it, only the build time does (the chunked walk repairs every chunk whose
+ * guessed start differs from its predecessor's end).  No upstream
+ * counterpart. */
+int rg_set_sweep_chunk(int64_t segments);
+
+/* Conservative 2D weights of n independent grid pairs built together: every
+ * stage runs once over all pairs (their sweep lines, chunks and output rows
+ * concatenated into one work queue), so the batch synchronises with the host
+ * a fixed number of times whatever n is.  Arrays of n device pointers / sizes
+ * as in rg_build_conservative_2d (d_w_in may be NULL, or hold NULL entries).
+ * out[g] receives pair g's handle and status[g] its status: a pair whose
+ * sweep fails (degenerate grids) gets RG_ERR_WALK and a NULL handle without
+ * affecting the others.  Returns RG_OK when the batch ran.  Results are bit
+ * for bit those of rg_build_conservative_2d on each pair.  No upstream
+ * counterpart (the upstream loops over elements in Python:
+ * regridding/_weights/_weights_conservative.py:110-139). */
+int rg_build_conservative_2d_batch(int64_t n, const double* const* d_xi, const double* const* d_yi,
+                                   const int64_t* nxi, const int64_t* nyi, const double* const* d_xo,
+                                   const double* const* d_yo, const int64_t* nxo, const int64_t* nyo,
+                                   const double* const* d_w_in, rg_stream_t stream, rg_weights* out,
+                                   int* status);
+
 /* Weights from entries in the upstream saved layout (one element):
  * indices_input, indices_output (int64, negative values count from the end as
  * in numpy), values (float64).  Entries of one output are applied in the

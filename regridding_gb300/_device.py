@@ -192,6 +192,63 @@ def build_conservative_2d(grid_input, grid_output, weights_input=None) -> Device
     return DeviceWeights(h, (nxo - 1, nyo - 1))
 
 
+def build_conservative_2d_batch(pairs, weights_input=None, max_cells: int = 48_000_000):
+    """Conservative weights of many (grid_input, grid_output) pairs built
+    together (``rg_build_conservative_2d_batch``): every stage of the build
+    runs once over all pairs of a sub-batch.  Sub-batches hold at most
+    ``max_cells`` input + output cells (the parallel walk's slot buffers scale
+    with the cells of a sub-batch).  Returns one DeviceWeights per pair, or
+    the RegridError of a pair whose build failed (degenerate grids), in
+    order."""
+    t = torch()
+    n = len(pairs)
+    if weights_input is None:
+        weights_input = [None] * n
+    dev = []
+    for (gi, go), wi in zip(pairs, weights_input):
+        xi, yi = (_as_device(a, t.float64) for a in gi)
+        xo, yo = (_as_device(a, t.float64) for a in go)
+        w = None if wi is None else _as_device(wi, t.float64)
+        dev.append((xi, yi, xo, yo, w))
+    results = [None] * n
+    start = 0
+    while start < n:
+        stop, cells = start, 0
+        while stop < n:
+            xi, _, xo, _, _ = dev[stop]
+            c = (xi.shape[0] - 1) * (xi.shape[1] - 1) + (xo.shape[0] - 1) * (xo.shape[1] - 1)
+            if stop > start and cells + c > max_cells:
+                break
+            cells += c
+            stop += 1
+        m = stop - start
+        P = ctypes.c_void_p * m
+        I = ctypes.c_int64 * m
+        part = dev[start:stop]
+        xi_p = P(*(a[0].data_ptr() for a in part))
+        yi_p = P(*(a[1].data_ptr() for a in part))
+        xo_p = P(*(a[2].data_ptr() for a in part))
+        yo_p = P(*(a[3].data_ptr() for a in part))
+        wi_p = P(*((a[4].data_ptr() if a[4] is not None else None) for a in part))
+        nxi = I(*(a[0].shape[0] for a in part))
+        nyi = I(*(a[0].shape[1] for a in part))
+        nxo = I(*(a[2].shape[0] for a in part))
+        nyo = I(*(a[2].shape[1] for a in part))
+        out = P()
+        status = (ctypes.c_int * m)()
+        _lib.call("rg_build_conservative_2d_batch", m, xi_p, yi_p, nxi, nyi, xo_p, yo_p, nxo, nyo,
+                  wi_p if any(a[4] is not None for a in part) else None, stream(), out, status)
+        for k in range(m):
+            if status[k] == _lib.RG_OK:
+                a = part[k]
+                results[start + k] = DeviceWeights(ctypes.c_void_p(out[k]), (a[2].shape[0] - 1, a[2].shape[1] - 1))
+            else:
+                results[start + k] = _lib.RegridError(
+                    f"conservative build of pair {start + k} failed (status {status[k]})")
+        start = stop
+    return results
+
+
 # ---------------------------------------------------------------------------
 # device-resident copies of saved weights, keyed by the identity of their
 # (read-only) numpy arrays

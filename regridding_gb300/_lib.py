@@ -34,6 +34,8 @@ SIGNATURES = {
     "rg_version": [],
     "rg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
     "rg_build_conservative_2d": [_P, _P, _I, _I, _P, _P, _I, _I, _P, _P, ctypes.POINTER(_P)],
+    "rg_set_sweep_chunk": [_I],
+    "rg_build_conservative_2d_batch": [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "rg_weights_from_coo": [_P, _P, _P, _I, _I, _I, _P, ctypes.POINTER(_P)],
     "rg_weights_info": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)],
     "rg_weights_set_output_shape": [_P, _I, _I],

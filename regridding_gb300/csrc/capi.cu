@@ -244,6 +244,46 @@ int rg_build_conservative_2d(const double* d_xi, const double* d_yi, int64_t nxi
     return RG_OK;
 }
 
+int rg_build_conservative_2d_batch(int64_t n, const double* const* d_xi, const double* const* d_yi,
+                                   const int64_t* nxi, const int64_t* nyi, const double* const* d_xo,
+                                   const double* const* d_yo, const int64_t* nxo, const int64_t* nyo,
+                                   const double* const* d_w_in, rg_stream_t stream, rg_weights* out,
+                                   int* status) {
+    RG_CHECK(n >= 1 && n < (1 << 24), RG_ERR_ARG, "rg_build_conservative_2d_batch: bad pair count %lld",
+             (long long)n);
+    RG_CHECK(d_xi && d_yi && nxi && nyi && d_xo && d_yo && nxo && nyo && out && status, RG_ERR_ARG,
+             "rg_build_conservative_2d_batch: NULL argument");
+    std::vector<PairSpec> pairs((size_t)n);
+    std::vector<rg_weights_s*> W((size_t)n, nullptr);
+    for (int64_t g = 0; g < n; g++) {
+        out[g] = nullptr;
+        status[g] = RG_ERR_ARG;
+        pairs[g] = PairSpec{d_xi[g], d_yi[g], nxi[g], nyi[g], d_xo[g], d_yo[g], nxo[g], nyo[g],
+                            d_w_in ? d_w_in[g] : nullptr};
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    for (int64_t g = 0; g < n; g++) {
+        W[g] = new (std::nothrow) rg_weights_s();
+        if (!W[g]) {
+            for (int64_t k = 0; k < g; k++) delete W[k];
+            RG_CHECK(false, RG_ERR_ALLOC, "host allocation failed");
+        }
+        W[g]->device = dev;
+    }
+    cudaStream_t s = (cudaStream_t)stream;
+    int st = build_batch(pairs.data(), (int)n, s, W.data(), status);
+    for (int64_t g = 0; g < n; g++) {
+        if (st == RG_OK && status[g] == RG_OK) {
+            out[g] = W[g];
+        } else {
+            if (st != RG_OK) status[g] = st;
+            free_weights(W[g], s);
+        }
+    }
+    return st;
+}
+
 int rg_weights_from_coo(const int64_t* d_in, const int64_t* d_out, const double* d_val, int64_t nnz,
                         int64_t n_in, int64_t n_out, rg_stream_t stream, rg_weights* out) {
     RG_CHECK(out, RG_ERR_ARG, "rg_weights_from_coo: out is NULL");

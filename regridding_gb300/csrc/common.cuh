@@ -159,3 +159,22 @@ struct rg_weights_s {
     int device = 0;
     std::mutex mu;  // guards the lazily made state above (made on first use by an apply)
 };
+
+namespace rg {
+
+// One grid pair of a conservative build (device pointers; row-major vertex
+// arrays of nx x ny; w_in nullable).
+struct PairSpec {
+    const double *xi, *yi;
+    int64_t nxi, nyi;
+    const double *xo, *yo;
+    int64_t nxo, nyo;
+    const double* w_in;
+};
+
+// Conservative weights of G pairs in one pass (conservative2d.cu); W[g] are
+// empty handles that receive the CSR of pair g when status[g] is RG_OK.
+int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, int* status);
+
+}  // namespace rg
+

@@ -27,9 +27,12 @@
 //     emission position) inside each bucket, and equal pairs are summed with
 //     numpy's add.reduceat association (first + pairwise rest), giving a CSR
 //     matrix whose values are bit-identical to the upstream coalesced ones.
+#include <algorithm>
+#include <atomic>
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <vector>
 
 #include "common.cuh"
 
@@ -440,11 +443,40 @@ __device__ __forceinline__ int family_of(const SweepParams& P, int64_t line) {
     return f;
 }
 
+// A batch of grid pairs swept together: per pair its sweep parameters and
+// chunk plan (whose line, chunk and slot bases are global across the batch),
+// prefix bases of its lines, chunks and output rows, and its own error word.
+// Kernels find their pair by binary search over the prefix bases.
+struct ChunkPlan;
+struct Batch {
+    const SweepParams* P;    // [G]
+    const ChunkPlan* C;      // [G] (null for whole-line walks)
+    const int64_t* line_base;   // [G + 1]
+    const int64_t* chunk_base;  // [G + 1]
+    const int64_t* out_base;    // [G + 1] first output row of every pair
+    unsigned* flags;            // [G]
+    int G;
+};
+
+// the pair owning global index x: the largest g with base[g] <= x
+__device__ __forceinline__ int pair_of(const int64_t* __restrict__ base, int G, int64_t x) {
+    int lo = 0, hi = G - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (base[mid] <= x) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
 // Starting state of every sweep line (:439-468): one warp per line.
-__global__ void __launch_bounds__(128) seat_kernel(SweepParams P, Seat* seats, unsigned* flags) {
+__global__ void __launch_bounds__(128) seat_kernel(Batch B, Seat* seats) {
     int lane = threadIdx.x & 31;
     int64_t line = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (line >= P.total_lines) return;
+    if (line >= B.line_base[B.G]) return;
+    const int pg = pair_of(B.line_base, B.G, line);
+    const SweepParams& P = B.P[pg];
+    unsigned* flags = B.flags + pg;
     const Family& F = P.fam[family_of(P, line)];
     const Static& S = P.st[F.st];
     int64_t li = line - F.line_base;
@@ -666,11 +698,13 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
 // triples a line emits; WRITE mode stores them from offsets[line].
 template <bool WRITE>
 __global__ void __launch_bounds__(64)
-    walk_kernel(SweepParams P, const Seat* __restrict__ seats, int64_t* __restrict__ counts,
+    walk_kernel(Batch B, const Seat* __restrict__ seats, int64_t* __restrict__ counts,
                 const int64_t* __restrict__ offsets, int32_t* __restrict__ raw_in,
-                int32_t* __restrict__ raw_out, double* __restrict__ raw_val, unsigned* flags) {
+                int32_t* __restrict__ raw_out, double* __restrict__ raw_val) {
     int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (line >= P.total_lines) return;
+    if (line >= B.line_base[B.G]) return;
+    const int pg = pair_of(B.line_base, B.G, line);
+    const SweepParams& P = B.P[pg];
     const Family F = P.fam[family_of(P, line)];
     const Static& S = P.st[F.st];
     Seat seat = seats[line];
@@ -678,8 +712,13 @@ __global__ void __launch_bounds__(64)
     const int64_t max_steps = 64 * (F.len + 4 * (S.ncx + S.ncy) + 16);
     int64_t n = walk_range<WRITE>(P, F, S, line - F.line_base, F.len - 1, state,
                                   WRITE ? offsets[line] : 0, WRITE ? offsets[line + 1] : 0, raw_in, raw_out,
-                                  raw_val, flags, max_steps);
+                                  raw_val, B.flags + pg, max_steps);
     if (!WRITE) counts[line] = n;
+    if (WRITE && B.out_base[pg] != 0) {
+        // output rows of the batch: the pair's rows follow those of the pairs before it
+        const int32_t ob = (int32_t)B.out_base[pg];
+        for (int64_t q = offsets[line]; q < offsets[line] + n; q++) raw_out[q] += ob;
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -779,10 +818,12 @@ __device__ WalkState guess_state(const Static& S, double px, double py, int64_t 
     return w;
 }
 
-__global__ void chunk_seat_kernel(SweepParams P, ChunkPlan C, const Seat* __restrict__ seats,
-                                  WalkState* __restrict__ starts) {
+__global__ void chunk_seat_kernel(Batch B, const Seat* __restrict__ seats, WalkState* __restrict__ starts) {
     int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (g >= C.chunk_base[4]) return;
+    if (g >= B.chunk_base[B.G]) return;
+    const int pg = pair_of(B.chunk_base, B.G, g);
+    const SweepParams& P = B.P[pg];
+    const ChunkPlan& C = B.C[pg];
     int f = family_of_chunk(C, g);
     const Family& F = P.fam[f];
     int64_t k = g - C.chunk_base[f];
@@ -802,11 +843,15 @@ __device__ __forceinline__ int64_t chunk_end(const ChunkPlan& C, const Family& F
 }
 
 __global__ void __launch_bounds__(64)
-    chunk_walk_kernel(SweepParams P, ChunkPlan C, const WalkState* __restrict__ starts,
-                      WalkState* __restrict__ ends, int64_t* __restrict__ counts, int32_t* __restrict__ s_in,
-                      int32_t* __restrict__ s_out, double* __restrict__ s_val, unsigned* flags) {
+    chunk_walk_kernel(Batch B, const WalkState* __restrict__ starts, WalkState* __restrict__ ends,
+                      int64_t* __restrict__ counts, int32_t* __restrict__ s_in, int32_t* __restrict__ s_out,
+                      double* __restrict__ s_val) {
     int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (g >= C.chunk_base[4]) return;
+    if (g >= B.chunk_base[B.G]) return;
+    const int pg = pair_of(B.chunk_base, B.G, g);
+    const SweepParams& P = B.P[pg];
+    const ChunkPlan& C = B.C[pg];
+    unsigned* flags = B.flags + pg;
     int f = family_of_chunk(C, g);
     const Family F = P.fam[f];
     const Static& S = P.st[F.st];
@@ -823,11 +868,15 @@ __global__ void __launch_bounds__(64)
 // One thread per line: walk chunks again, in order, wherever a chunk's start
 // differs from the previous chunk's end.
 __global__ void __launch_bounds__(64)
-    chunk_repair_kernel(SweepParams P, ChunkPlan C, WalkState* __restrict__ starts, WalkState* __restrict__ ends,
+    chunk_repair_kernel(Batch B, WalkState* __restrict__ starts, WalkState* __restrict__ ends,
                         int64_t* __restrict__ counts, int32_t* __restrict__ s_in, int32_t* __restrict__ s_out,
-                        double* __restrict__ s_val, unsigned* flags, unsigned long long* __restrict__ n_repaired) {
+                        double* __restrict__ s_val, unsigned long long* __restrict__ n_repaired) {
     int64_t line = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (line >= P.total_lines) return;
+    if (line >= B.line_base[B.G]) return;
+    const int pg = pair_of(B.line_base, B.G, line);
+    const SweepParams& P = B.P[pg];
+    const ChunkPlan& C = B.C[pg];
+    unsigned* flags = B.flags + pg;
     int f = family_of(P, line);
     const Family F = P.fam[f];
     const Static& S = P.st[F.st];
@@ -852,20 +901,24 @@ __global__ void __launch_bounds__(64)
 
 // One warp per chunk: move its triples from its slots to their place in the
 // emission order.
-__global__ void chunk_compact_kernel(ChunkPlan C, const int64_t* __restrict__ counts,
+__global__ void chunk_compact_kernel(Batch B, const int64_t* __restrict__ counts,
                                      const int64_t* __restrict__ offsets, const int32_t* __restrict__ s_in,
                                      const int32_t* __restrict__ s_out, const double* __restrict__ s_val,
                                      int32_t* __restrict__ raw_in, int32_t* __restrict__ raw_out,
                                      double* __restrict__ raw_val) {
     int lane = threadIdx.x & 31;
     int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (g >= C.chunk_base[4]) return;
+    if (g >= B.chunk_base[B.G]) return;
+    const int pg = pair_of(B.chunk_base, B.G, g);
+    const ChunkPlan& C = B.C[pg];
+    // output rows of the batch: the pair's rows follow those of the pairs before it
+    const int32_t ob = (int32_t)B.out_base[pg];
     int f = family_of_chunk(C, g);
     int64_t base = C.slot_base[f] + (g - C.chunk_base[f]) * C.cap[f];
     int64_t n = counts[g], dst = offsets[g];
     for (int64_t q = lane; q < n; q += 32) {
         raw_in[dst + q] = s_in[base + q];
-        raw_out[dst + q] = s_out[base + q];
+        raw_out[dst + q] = s_out[base + q] + ob;
         raw_val[dst + q] = s_val[base + q];
     }
 }
@@ -989,9 +1042,21 @@ __global__ void compact_rows(const int64_t* __restrict__ bptr, const int64_t* __
     }
 }
 
-int prepare_static(const double* x, const double* y, int64_t nx, int64_t ny, const double* bbox_h,
-                   Static* S, Edge** edges_out, int32_t** ptr_out, int32_t** items_out,
-                   cudaStream_t s) {
+// Static-grid preparation in two halves so that a batch synchronises once
+// for all its grids: the first half fills the boundary edges, sizes the
+// bins and counts the edges of every bin (the total lands in *total_dev);
+// the second, after the caller has read the totals, files the edges.
+struct StaticPrep {
+    Edge* edges = nullptr;
+    unsigned* counts = nullptr;
+    int64_t* ptr64 = nullptr;
+    int32_t* ptr32 = nullptr;
+    int32_t* items = nullptr;
+    int64_t nedges = 0, nbins = 0;
+};
+
+int prepare_static_count(const double* x, const double* y, int64_t nx, int64_t ny, const double* bbox_h, Static* S,
+                         StaticPrep* R, int64_t* total_dev, cudaStream_t s) {
     S->g = Grid{x, y, nx, ny};
     S->ncx = nx - 1;
     S->ncy = ny - 1;
@@ -1000,12 +1065,11 @@ int prepare_static(const double* x, const double* y, int64_t nx, int64_t ny, con
     S->bux = bbox_h[2];
     S->buy = bbox_h[3];
     S->nbound = 2 * (nx - 1) + 2 * (ny - 1);
-    int64_t nedges = 2 * S->ncy + 2 * S->ncx;
-    Edge* edges = nullptr;
-    RG_TRY(dalloc(&edges, (size_t)nedges, s));
-    *edges_out = edges;
-    boundary_edges_kernel<<<grid_for(nedges, 128), 128, 0, s>>>(S->g, edges, nedges);
-    S->edges = edges;
+    const int64_t nedges = 2 * S->ncy + 2 * S->ncx;
+    R->nedges = nedges;
+    RG_TRY(dalloc(&R->edges, (size_t)nedges, s));
+    boundary_edges_kernel<<<grid_for(nedges, 128), 128, 0, s>>>(S->g, R->edges, nedges);
+    S->edges = R->edges;
     // bins: square, sized so that a bin holds about one edge along the boundary
     double ex = S->bux - S->blx, ey = S->buy - S->bly;
     double ext = ex > ey ? ex : ey;
@@ -1019,40 +1083,46 @@ int prepare_static(const double* x, const double* y, int64_t nx, int64_t ny, con
     b.inv_h = 1.0 / hbin;
     b.nbx = (int)std::min<double>(1024.0, std::max(1.0, std::ceil(ex / hbin)));
     b.nby = (int)std::min<double>(1024.0, std::max(1.0, std::ceil(ey / hbin)));
-    if (!std::isfinite(ex) || !std::isfinite(ey)) { b.nbx = 1; b.nby = 1; }
-    int64_t nbins = (int64_t)b.nbx * b.nby;
-    unsigned* counts = nullptr;
-    int64_t* ptr64 = nullptr;
-    int32_t *ptr32 = nullptr, *items = nullptr;
-    int64_t* total_dev = nullptr;
-    RG_TRY(dalloc(&counts, (size_t)nbins + 1, s));
-    RG_TRY(dalloc(&ptr64, (size_t)nbins + 1, s));
-    RG_TRY(dalloc(&ptr32, (size_t)nbins + 1, s));
-    RG_TRY(dalloc(&total_dev, 1, s));
-    RG_CUDA(cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbins + 1), s));
+    if (!std::isfinite(ex) || !std::isfinite(ey)) {
+        b.nbx = 1;
+        b.nby = 1;
+    }
     b.ptr = nullptr;
     b.items = nullptr;
-    bin_edges_kernel<false><<<grid_for(nedges, 128), 128, 0, s>>>(edges, nedges, b, counts, nullptr,
-                                                                   nullptr);
-    RG_TRY(exclusive_scan_u32_to_i64(counts, ptr64, nbins + 1, total_dev, s));
-    int64_t total = 0;
-    RG_CUDA(cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s));
-    RG_CUDA(cudaStreamSynchronize(s));
-    RG_TRY(dalloc(&items, (size_t)total, s));
-    RG_CUDA(cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbins + 1), s));
-    bin_edges_kernel<true><<<grid_for(nedges, 128), 128, 0, s>>>(edges, nedges, b, counts, items,
-                                                                  ptr64);
-    i64_to_i32<<<grid_for(nbins + 1, 256), 256, 0, s>>>(ptr64, ptr32, nbins + 1);
-    RG_CUDA(cudaGetLastError());
-    dfree(counts, s);
-    dfree(ptr64, s);
-    dfree(total_dev, s);
-    b.ptr = ptr32;
-    b.items = items;
     S->bins = b;
-    *ptr_out = ptr32;
-    *items_out = items;
+    const int64_t nbins = (int64_t)b.nbx * b.nby;
+    R->nbins = nbins;
+    RG_TRY(dalloc(&R->counts, (size_t)nbins + 1, s));
+    RG_TRY(dalloc(&R->ptr64, (size_t)nbins + 1, s));
+    RG_TRY(dalloc(&R->ptr32, (size_t)nbins + 1, s));
+    RG_CUDA(cudaMemsetAsync(R->counts, 0, sizeof(unsigned) * (nbins + 1), s));
+    bin_edges_kernel<false><<<grid_for(nedges, 128), 128, 0, s>>>(R->edges, nedges, b, R->counts, nullptr, nullptr);
+    return exclusive_scan_u32_to_i64(R->counts, R->ptr64, nbins + 1, total_dev, s);
+}
+
+int prepare_static_fill(Static* S, StaticPrep* R, int64_t total, cudaStream_t s) {
+    RG_TRY(dalloc(&R->items, (size_t)total, s));
+    RG_CUDA(cudaMemsetAsync(R->counts, 0, sizeof(unsigned) * (R->nbins + 1), s));
+    bin_edges_kernel<true><<<grid_for(R->nedges, 128), 128, 0, s>>>(R->edges, R->nedges, S->bins, R->counts,
+                                                                     R->items, R->ptr64);
+    i64_to_i32<<<grid_for(R->nbins + 1, 256), 256, 0, s>>>(R->ptr64, R->ptr32, R->nbins + 1);
+    RG_CUDA(cudaGetLastError());
+    dfree(R->counts, s);
+    dfree(R->ptr64, s);
+    R->counts = nullptr;
+    R->ptr64 = nullptr;
+    S->bins.ptr = R->ptr32;
+    S->bins.items = R->items;
     return RG_OK;
+}
+
+void free_static(StaticPrep* R, cudaStream_t s) {
+    dfree(R->edges, s);
+    dfree(R->counts, s);
+    dfree(R->ptr64, s);
+    dfree(R->ptr32, s);
+    dfree(R->items, s);
+    *R = StaticPrep();
 }
 
 }  // namespace
@@ -1096,9 +1166,12 @@ int locate_2d_exact(const double* x, const double* y, int64_t nx, int64_t ny, co
     return RG_OK;
 }
 
+std::atomic<int64_t> g_sweep_chunk{32};
+
 namespace {
 
-int check_walk_flags(unsigned fl) {
+// The walk failures a grid's error word records, as a status (message set).
+int walk_status(unsigned fl) {
     if (fl & (FLAG_WALK_CAP | FLAG_SEAT_OUTSIDE)) {
         set_error("conservative sweep: %s",
                   (fl & FLAG_WALK_CAP) ? "a grid line exceeded its step cap (degenerate grids?)"
@@ -1109,30 +1182,34 @@ int check_walk_flags(unsigned fl) {
     return RG_OK;
 }
 
-// One thread per line, count then write (synchronises once).
-int sweep_lines(const SweepParams& P, const Seat* seats, unsigned* flags, int64_t* total_dev, cudaStream_t s,
-                int32_t** raw_in, int32_t** raw_out, double** raw_val, int64_t* nraw_out) {
-    const int64_t base = P.total_lines;
+template <typename T>
+int upload(T** d, const std::vector<T>& h, cudaStream_t s) {
+    RG_TRY(dalloc(d, h.size(), s));
+    RG_CUDA(cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s));
+    return RG_OK;
+}
+
+// One thread per line over all lines of the batch, count then write
+// (synchronises once).  fl receives every grid's error word.
+int sweep_lines(const Batch& B, int64_t lines, const Seat* seats, int64_t* total_dev, cudaStream_t s,
+                int32_t** raw_in, int32_t** raw_out, double** raw_val, int64_t* nraw_out, std::vector<unsigned>& fl) {
     int64_t *counts = nullptr, *offsets = nullptr;
     int st = RG_OK;
     do {
-        if ((st = dalloc(&counts, (size_t)base + 1, s))) break;
-        if ((st = dalloc(&offsets, (size_t)base + 1, s))) break;
-        walk_kernel<false><<<grid_for(base, 64), 64, 0, s>>>(P, seats, counts, nullptr, nullptr, nullptr, nullptr,
-                                                             flags);
-        cudaMemsetAsync(counts + base, 0, sizeof(int64_t), s);
-        if ((st = exclusive_scan_i64(counts, offsets, base + 1, total_dev, s))) break;
+        if ((st = dalloc(&counts, (size_t)lines + 1, s))) break;
+        if ((st = dalloc(&offsets, (size_t)lines + 1, s))) break;
+        walk_kernel<false><<<grid_for(lines, 64), 64, 0, s>>>(B, seats, counts, nullptr, nullptr, nullptr, nullptr);
+        cudaMemsetAsync(counts + lines, 0, sizeof(int64_t), s);
+        if ((st = exclusive_scan_i64(counts, offsets, lines + 1, total_dev, s))) break;
         int64_t nraw = 0;
-        unsigned fl = 0;
         cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(fl.data(), B.flags, sizeof(unsigned) * fl.size(), cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative sweep (count walk): %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
             break;
         }
-        if ((st = check_walk_flags(fl))) break;
         if (nraw >= (int64_t)UINT32_MAX) {
             set_error("conservative sweep: %lld raw entries exceed 2^32", (long long)nraw);
             st = RG_ERR_UNSUPPORTED;
@@ -1141,8 +1218,7 @@ int sweep_lines(const SweepParams& P, const Seat* seats, unsigned* flags, int64_
         if ((st = dalloc(raw_in, (size_t)nraw, s))) break;
         if ((st = dalloc(raw_out, (size_t)nraw, s))) break;
         if ((st = dalloc(raw_val, (size_t)nraw, s))) break;
-        walk_kernel<true><<<grid_for(base, 64), 64, 0, s>>>(P, seats, nullptr, offsets, *raw_in, *raw_out,
-                                                            *raw_val, flags);
+        walk_kernel<true><<<grid_for(lines, 64), 64, 0, s>>>(B, seats, nullptr, offsets, *raw_in, *raw_out, *raw_val);
         *nraw_out = nraw;
     } while (0);
     dfree(counts, s);
@@ -1150,36 +1226,48 @@ int sweep_lines(const SweepParams& P, const Seat* seats, unsigned* flags, int64_
     return st;
 }
 
-// Chunked walk (see chunk_walk_kernel).  Sets *nraw_out to -1 (and frees
-// everything) when a chunk needed more slots than it was given.
-int sweep_chunked(const SweepParams& P, const Seat* seats, const double* bbox_h, unsigned* flags,
-                  int64_t* total_dev, cudaStream_t s, int32_t** raw_in, int32_t** raw_out, double** raw_val,
-                  int64_t* nraw_out) {
-    ChunkPlan C;
-    memset(&C, 0, sizeof(C));
-    // sweep segments per chunk; RG_SWEEP_CHUNK overrides (0 walks whole lines)
-    C.ch = 32;
-    if (const char* env = getenv("RG_SWEEP_CHUNK")) C.ch = atoll(env);
+// Chunked walk over all lines of the batch (see chunk_walk_kernel).  Sets
+// *nraw_out to -1 (and frees everything) when a chunk needed more slots than
+// it was given or the slots would not fit; fl receives every grid's error word.
+int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector<double>& bbox_h,
+                  const Seat* seats, int64_t lines, int64_t* total_dev, cudaStream_t s, int32_t** raw_in,
+                  int32_t** raw_out, double** raw_val, int64_t* nraw_out, std::vector<unsigned>& fl,
+                  ChunkPlan** plans_dev, int64_t** chunk_base_dev) {
+    const int G = B.G;
+    // sweep segments per chunk: rg_set_sweep_chunk (default 32), the
+    // RG_SWEEP_CHUNK environment variable overriding it (0 walks whole lines)
+    int64_t ch = g_sweep_chunk.load();
+    if (const char* env = getenv("RG_SWEEP_CHUNK")) ch = atoll(env);
     *nraw_out = -1;
-    if (C.ch <= 0) return RG_OK;
+    if (ch <= 0) return RG_OK;
+    std::vector<ChunkPlan> C((size_t)G);
+    std::vector<int64_t> chunk_base((size_t)G + 1, 0);
     int64_t chunks = 0, slots = 0;
-    for (int f = 0; f < 4; f++) {
-        const Family& F = P.fam[f];
-        const Static& S = P.st[F.st];
-        const double* bs = F.sweep_input ? bbox_h : bbox_h + 4;  // sweep grid's box
-        const double* bt = F.sweep_input ? bbox_h + 4 : bbox_h;  // static grid's box
-        double seg = fmax(bs[2] - bs[0], bs[3] - bs[1]) / (double)(F.len - 1 > 0 ? F.len - 1 : 1);
-        double dens = fmax((double)S.ncx / fmax(bt[2] - bt[0], 1e-300), (double)S.ncy / fmax(bt[3] - bt[1], 1e-300));
-        double cross = 2.0 * ceil(1.5 * seg * dens) + 2.0;
-        if (!(cross < 1e6)) cross = 1e6;
-        C.nc[f] = (F.len - 1 + C.ch - 1) / C.ch;
-        C.chunk_base[f] = chunks;
-        C.cap[f] = 2 * C.ch * (1 + (int64_t)cross) + 32;
-        C.slot_base[f] = slots;
-        chunks += F.lines * C.nc[f];
-        slots += F.lines * C.nc[f] * C.cap[f];
+    for (int g = 0; g < G; g++) {
+        ChunkPlan& c = C[g];
+        memset(&c, 0, sizeof(c));
+        c.ch = ch;
+        chunk_base[g] = chunks;
+        const double* bb = bbox_h.data() + 8 * g;
+        for (int f = 0; f < 4; f++) {
+            const Family& F = P[g].fam[f];
+            const Static& S = P[g].st[F.st];
+            const double* bs = F.sweep_input ? bb : bb + 4;  // sweep grid's box
+            const double* bt = F.sweep_input ? bb + 4 : bb;  // static grid's box
+            double seg = fmax(bs[2] - bs[0], bs[3] - bs[1]) / (double)(F.len - 1 > 0 ? F.len - 1 : 1);
+            double dens = fmax((double)S.ncx / fmax(bt[2] - bt[0], 1e-300), (double)S.ncy / fmax(bt[3] - bt[1], 1e-300));
+            double cross = 2.0 * ceil(1.5 * seg * dens) + 2.0;
+            if (!(cross < 1e6)) cross = 1e6;
+            c.nc[f] = (F.len - 1 + ch - 1) / ch;
+            c.chunk_base[f] = chunks;
+            c.cap[f] = 2 * ch * (1 + (int64_t)cross) + 32;
+            c.slot_base[f] = slots;
+            chunks += F.lines * c.nc[f];
+            slots += F.lines * c.nc[f] * c.cap[f];
+        }
+        c.chunk_base[4] = chunks;
     }
-    C.chunk_base[4] = chunks;
+    chunk_base[G] = chunks;
     if (slots * 16 > (int64_t)24 << 30 || slots >= (int64_t)1 << 40) return RG_OK;  // too big: walk lines
 
     WalkState *starts = nullptr, *ends = nullptr;
@@ -1190,6 +1278,10 @@ int sweep_chunked(const SweepParams& P, const Seat* seats, const double* bbox_h,
     int st = RG_OK;
     bool overflow = false;
     do {
+        if ((st = upload(plans_dev, C, s))) break;
+        if ((st = upload(chunk_base_dev, chunk_base, s))) break;
+        B.C = *plans_dev;
+        B.chunk_base = *chunk_base_dev;
         if ((st = dalloc(&starts, (size_t)chunks, s))) break;
         if ((st = dalloc(&ends, (size_t)chunks, s))) break;
         if ((st = dalloc(&counts, (size_t)chunks + 1, s))) break;
@@ -1199,26 +1291,25 @@ int sweep_chunked(const SweepParams& P, const Seat* seats, const double* bbox_h,
         if ((st = dalloc(&s_out, (size_t)slots, s))) break;
         if ((st = dalloc(&s_val, (size_t)slots, s))) break;
         cudaMemsetAsync(n_rep, 0, sizeof(unsigned long long), s);
-        chunk_seat_kernel<<<grid_for(chunks, 128), 128, 0, s>>>(P, C, seats, starts);
-        chunk_walk_kernel<<<grid_for(chunks, 64), 64, 0, s>>>(P, C, starts, ends, counts, s_in, s_out, s_val, flags);
-        chunk_repair_kernel<<<grid_for(P.total_lines, 64), 64, 0, s>>>(P, C, starts, ends, counts, s_in, s_out,
-                                                                      s_val, flags, n_rep);
+        chunk_seat_kernel<<<grid_for(chunks, 128), 128, 0, s>>>(B, seats, starts);
+        chunk_walk_kernel<<<grid_for(chunks, 64), 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val);
+        chunk_repair_kernel<<<grid_for(lines, 64), 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val, n_rep);
         cudaMemsetAsync(counts + chunks, 0, sizeof(int64_t), s);
         if ((st = exclusive_scan_i64(counts, offsets, chunks + 1, total_dev, s))) break;
         int64_t nraw = 0;
-        unsigned fl = 0;
         cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaMemcpyAsync(fl.data(), B.flags, sizeof(unsigned) * fl.size(), cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative sweep (chunked walk): %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
             break;
         }
-        if ((st = check_walk_flags(fl))) break;
-        if (fl & FLAG_CAPACITY) {
+        bool cap = false;
+        for (unsigned f : fl) cap = cap || (f & FLAG_CAPACITY);
+        if (cap) {
             overflow = true;
-            cudaMemsetAsync(flags, 0, sizeof(unsigned), s);
+            cudaMemsetAsync(B.flags, 0, sizeof(unsigned) * fl.size(), s);
             break;
         }
         if (nraw >= (int64_t)UINT32_MAX) {
@@ -1229,7 +1320,7 @@ int sweep_chunked(const SweepParams& P, const Seat* seats, const double* bbox_h,
         if ((st = dalloc(raw_in, (size_t)nraw, s))) break;
         if ((st = dalloc(raw_out, (size_t)nraw, s))) break;
         if ((st = dalloc(raw_val, (size_t)nraw, s))) break;
-        chunk_compact_kernel<<<grid_for(chunks * 32, 256), 256, 0, s>>>(C, counts, offsets, s_in, s_out, s_val,
+        chunk_compact_kernel<<<grid_for(chunks * 32, 256), 256, 0, s>>>(B, counts, offsets, s_in, s_out, s_val,
                                                                         *raw_in, *raw_out, *raw_val);
         e = cudaGetLastError();
         if (e != cudaSuccess) {
@@ -1251,25 +1342,70 @@ int sweep_chunked(const SweepParams& P, const Seat* seats, const double* bbox_h,
     return st;
 }
 
+// Per-grid sizes of the merged CSR: nnz_base[g] = row_ptr[out_base[g]].
+__global__ void nnz_bases(const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ out_base, int G,
+                          int64_t* __restrict__ nnz_base) {
+    for (int g = blockIdx.x * blockDim.x + threadIdx.x; g <= G; g += gridDim.x * blockDim.x)
+        nnz_base[g] = row_ptr[out_base[g]];
+}
+
+// Copy every grid's rows and entries of the merged CSR to its own arrays.
+__global__ void split_rows(const int64_t* __restrict__ row_ptr, const int64_t* __restrict__ out_base,
+                           const int64_t* __restrict__ nnz_base, int G, int64_t* const* __restrict__ dst_row_ptr) {
+    const int64_t n = out_base[G];
+    for (int64_t r = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; r < n; r += (int64_t)gridDim.x * blockDim.x) {
+        const int g = pair_of(out_base, G, r);
+        const int64_t local = r - out_base[g];
+        dst_row_ptr[g][local] = row_ptr[r] - nnz_base[g];
+        if (r + 1 == out_base[g + 1]) dst_row_ptr[g][local + 1] = row_ptr[r + 1] - nnz_base[g];
+    }
+}
+__global__ void split_entries(const int32_t* __restrict__ col, const double* __restrict__ val,
+                              const int64_t* __restrict__ nnz_base, int G, int32_t* const* __restrict__ dst_col,
+                              double* const* __restrict__ dst_val) {
+    const int64_t n = nnz_base[G];
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x) {
+        const int g = pair_of(nnz_base, G, k);
+        const int64_t local = k - nnz_base[g];
+        dst_col[g][local] = col[k];
+        dst_val[g][local] = val[k];
+    }
+}
+
 }  // namespace
 
-int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64_t nyi,
-                          const double* xo, const double* yo, int64_t nxo, int64_t nyo,
-                          const double* w_in, cudaStream_t s, rg_weights_s* W) {
-    RG_CHECK(nxi >= 2 && nyi >= 2 && nxo >= 2 && nyo >= 2, RG_ERR_ARG,
-             "conservative 2D grids need at least 2 vertices per axis");
-    int64_t ncx_in = nxi - 1, ncy_in = nyi - 1, ncx_out = nxo - 1, ncy_out = nyo - 1;
-    int64_t n_in = ncx_in * ncy_in, n_out = ncx_out * ncy_out;
-    RG_CHECK(n_in < INT32_MAX && n_out < INT32_MAX, RG_ERR_UNSUPPORTED,
-             "grids above 2^31 cells are not supported");
+// Conservative weights of G grid pairs in one pass: every stage runs once
+// over all pairs (their lines, chunks and output rows concatenated), and the
+// batch synchronises with the host five times whatever G is.  W[g] receives
+// pair g's CSR when status[g] is RG_OK; a pair whose sweep fails (degenerate
+// grids) gets its error in status[g] and leaves the others unaffected.
+int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, int* status) {
+    RG_CHECK(G >= 1, RG_ERR_ARG, "conservative batch: no grid pairs");
+    std::vector<int64_t> in_base((size_t)G + 1, 0), out_base((size_t)G + 1, 0), line_base((size_t)G + 1, 0);
+    for (int g = 0; g < G; g++) {
+        const PairSpec& q = pairs[g];
+        RG_CHECK(q.nxi >= 2 && q.nyi >= 2 && q.nxo >= 2 && q.nyo >= 2, RG_ERR_ARG,
+                 "conservative 2D grids need at least 2 vertices per axis");
+        const int64_t n_in = (q.nxi - 1) * (q.nyi - 1), n_out = (q.nxo - 1) * (q.nyo - 1);
+        in_base[g + 1] = in_base[g] + n_in;
+        out_base[g + 1] = out_base[g] + n_out;
+        // lines of the four families: output rows/columns, then input rows/columns
+        line_base[g + 1] = line_base[g] + q.nyo + q.nxo + q.nyi + q.nxi;
+        status[g] = RG_OK;
+    }
+    RG_CHECK(in_base[G] < INT32_MAX && out_base[G] < INT32_MAX, RG_ERR_UNSUPPORTED,
+             "grids above 2^31 cells (in a batch, in total) are not supported");
+    const int64_t lines = line_base[G], n_out_all = out_base[G];
 
     int st = RG_OK;
     double* area_in = nullptr;
     double* bbox_d = nullptr;
     double* bbox_part = nullptr;
-    Edge* edges[2] = {nullptr, nullptr};
-    int32_t* bptr[2] = {nullptr, nullptr};
-    int32_t* bitems[2] = {nullptr, nullptr};
+    std::vector<StaticPrep> prep((size_t)2 * G);
+    int64_t* totals = nullptr;
+    SweepParams* P_dev = nullptr;
+    int64_t *line_base_dev = nullptr, *out_base_dev = nullptr, *chunk_base_dev = nullptr;
+    ChunkPlan* plans_dev = nullptr;
     Seat* seats = nullptr;
     int64_t* total_dev = nullptr;
     unsigned* flags = nullptr;
@@ -1281,123 +1417,243 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
     int32_t* tmp_col = nullptr;
     double* tmp_val = nullptr;
     int64_t* row_nnz = nullptr;
+    int64_t* row_ptr = nullptr;
+    int32_t* col = nullptr;
+    double* val = nullptr;
+    int64_t* nnz_base_dev = nullptr;
+    void** dst_dev = nullptr;  // [3G]: row_ptr, col, val pointers of every grid
 
     do {
-        if ((st = dalloc(&area_in, (size_t)n_in, s))) break;
-        if ((st = cell_area_2d(xi, yi, nxi, nyi, area_in, s))) break;
-        if ((st = dalloc(&bbox_d, 8, s))) break;
+        // areas of the input cells and bounding boxes of all grids (sync 1)
+        if ((st = dalloc(&area_in, (size_t)in_base[G], s))) break;
+        if ((st = dalloc(&bbox_d, (size_t)8 * G, s))) break;
         if ((st = dalloc(&bbox_part, 8 * 256, s))) break;
-        if ((st = dalloc(&flags, 1, s))) break;
-        if ((st = dalloc(&total_dev, 1, s))) break;
-        cudaMemsetAsync(flags, 0, sizeof(unsigned), s);
-        bbox_partial<<<256, 256, 0, s>>>(xi, yi, nxi * nyi, bbox_part);
-        bbox_combine<<<1, 32, 0, s>>>(bbox_part, 256, bbox_d);
-        bbox_partial<<<256, 256, 0, s>>>(xo, yo, nxo * nyo, bbox_part + 4 * 256);
-        bbox_combine<<<1, 32, 0, s>>>(bbox_part + 4 * 256, 256, bbox_d + 4);
-        double bbox_h[8];
-        cudaMemcpyAsync(bbox_h, bbox_d, sizeof(bbox_h), cudaMemcpyDeviceToHost, s);
+        for (int g = 0; g < G && st == RG_OK; g++) {
+            const PairSpec& q = pairs[g];
+            st = cell_area_2d(q.xi, q.yi, q.nxi, q.nyi, area_in + in_base[g], s);
+            bbox_partial<<<256, 256, 0, s>>>(q.xi, q.yi, q.nxi * q.nyi, bbox_part);
+            bbox_combine<<<1, 32, 0, s>>>(bbox_part, 256, bbox_d + 8 * g);
+            bbox_partial<<<256, 256, 0, s>>>(q.xo, q.yo, q.nxo * q.nyo, bbox_part + 4 * 256);
+            bbox_combine<<<1, 32, 0, s>>>(bbox_part + 4 * 256, 256, bbox_d + 8 * g + 4);
+        }
+        if (st) break;
+        std::vector<double> bbox_h((size_t)8 * G);
+        cudaMemcpyAsync(bbox_h.data(), bbox_d, sizeof(double) * 8 * G, cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
-            set_error("build_conservative_2d: %s", cudaGetErrorString(e));
+            set_error("conservative build: %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
             break;
         }
 
-        SweepParams P;
-        memset(&P, 0, sizeof(P));
-        if ((st = prepare_static(xi, yi, nxi, nyi, bbox_h, &P.st[0], &edges[0], &bptr[0], &bitems[0], s)))
-            break;
-        if ((st = prepare_static(xo, yo, nxo, nyo, bbox_h + 4, &P.st[1], &edges[1], &bptr[1], &bitems[1],
-                                 s)))
-            break;
-        // families in upstream order: sweep output (axis 0, 1), sweep input (axis 0, 1)
-        int64_t base = 0;
-        for (int k = 0; k < 4; k++) {
-            Family& F = P.fam[k];
-            F.sweep_input = k >= 2;
-            F.axis = k & 1;
-            F.sweep = F.sweep_input ? Grid{xi, yi, nxi, nyi} : Grid{xo, yo, nxo, nyo};
-            F.st = F.sweep_input ? 1 : 0;
-            F.transposed = F.axis == 0;
-            F.lines = F.axis == 0 ? F.sweep.ny : F.sweep.nx;
-            F.len = F.axis == 0 ? F.sweep.nx : F.sweep.ny;
-            F.line_base = base;
-            base += F.lines;
+        // static grids: boundary edges and bins (sync 2)
+        std::vector<SweepParams> P((size_t)G);
+        if ((st = dalloc(&totals, (size_t)2 * G, s))) break;
+        for (int g = 0; g < G && st == RG_OK; g++) {
+            const PairSpec& q = pairs[g];
+            memset(&P[g], 0, sizeof(SweepParams));
+            st = prepare_static_count(q.xi, q.yi, q.nxi, q.nyi, bbox_h.data() + 8 * g, &P[g].st[0], &prep[2 * g],
+                                      totals + 2 * g, s);
+            if (st == RG_OK)
+                st = prepare_static_count(q.xo, q.yo, q.nxo, q.nyo, bbox_h.data() + 8 * g + 4, &P[g].st[1],
+                                          &prep[2 * g + 1], totals + 2 * g + 1, s);
         }
-        P.total_lines = base;
-        P.area_in = area_in;
-        P.w_in = w_in;
-        P.ncy_in = ncy_in;
-        P.ncy_out = ncy_out;
+        if (st) break;
+        std::vector<int64_t> totals_h((size_t)2 * G);
+        cudaMemcpyAsync(totals_h.data(), totals, sizeof(int64_t) * 2 * G, cudaMemcpyDeviceToHost, s);
+        e = cudaStreamSynchronize(s);
+        if (e != cudaSuccess) {
+            set_error("conservative build: %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        for (int g = 0; g < G && st == RG_OK; g++) {
+            st = prepare_static_fill(&P[g].st[0], &prep[2 * g], totals_h[2 * g], s);
+            if (st == RG_OK) st = prepare_static_fill(&P[g].st[1], &prep[2 * g + 1], totals_h[2 * g + 1], s);
+        }
+        if (st) break;
 
-        if ((st = dalloc(&seats, (size_t)base, s))) break;
-        seat_kernel<<<grid_for(base * 32, 128), 128, 0, s>>>(P, seats, flags);
+        // sweep families in upstream order: sweep output (axis 0, 1), sweep
+        // input (axis 0, 1); line bases global across the batch
+        for (int g = 0; g < G; g++) {
+            const PairSpec& q = pairs[g];
+            int64_t base = line_base[g];
+            for (int k = 0; k < 4; k++) {
+                Family& F = P[g].fam[k];
+                F.sweep_input = k >= 2;
+                F.axis = k & 1;
+                F.sweep = F.sweep_input ? Grid{q.xi, q.yi, q.nxi, q.nyi} : Grid{q.xo, q.yo, q.nxo, q.nyo};
+                F.st = F.sweep_input ? 1 : 0;
+                F.transposed = F.axis == 0;
+                F.lines = F.axis == 0 ? F.sweep.ny : F.sweep.nx;
+                F.len = F.axis == 0 ? F.sweep.nx : F.sweep.ny;
+                F.line_base = base;
+                base += F.lines;
+            }
+            P[g].total_lines = base;
+            P[g].area_in = area_in + in_base[g];
+            P[g].w_in = q.w_in;
+            P[g].ncy_in = q.nyi - 1;
+            P[g].ncy_out = q.nyo - 1;
+        }
+        if ((st = upload(&P_dev, P, s))) break;
+        if ((st = upload(&line_base_dev, line_base, s))) break;
+        if ((st = upload(&out_base_dev, out_base, s))) break;
+        if ((st = dalloc(&flags, (size_t)G, s))) break;
+        if ((st = dalloc(&total_dev, 1, s))) break;
+        cudaMemsetAsync(flags, 0, sizeof(unsigned) * G, s);
+        Batch B;
+        B.P = P_dev;
+        B.C = nullptr;
+        B.line_base = line_base_dev;
+        B.chunk_base = nullptr;
+        B.out_base = out_base_dev;
+        B.flags = flags;
+        B.G = G;
+
+        // seats and the sweep (sync 3)
+        if ((st = dalloc(&seats, (size_t)lines, s))) break;
+        seat_kernel<<<grid_for(lines * 32, 128), 128, 0, s>>>(B, seats);
+        std::vector<unsigned> fl((size_t)G, 0u);
         int64_t nraw = 0;
-        if ((st = sweep_chunked(P, seats, bbox_h, flags, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw)))
+        if ((st = sweep_chunked(B, P, bbox_h, seats, lines, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw, fl,
+                                &plans_dev, &chunk_base_dev)))
             break;
         if (nraw < 0) {
             // a chunk overflowed its slots: walk whole lines instead
-            if ((st = sweep_lines(P, seats, flags, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw))) break;
+            if ((st = sweep_lines(B, lines, seats, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw, fl))) break;
         }
-        unsigned fl = 0;
-        // merge
+        for (int g = 0; g < G; g++) status[g] = walk_status(fl[g]);
+
+        // merge: one bucket sort over the output rows of the whole batch
+        // (sync 4 for the entry count; the per-grid sizes come with it)
         if ((st = dalloc(&skey, (size_t)nraw, s))) break;
-        cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
-        if ((st = dalloc(&bucket_ptr, (size_t)n_out + 1, s))) break;
+        if ((st = dalloc(&bucket_ptr, (size_t)n_out_all + 1, s))) break;
         if ((st = dalloc(&perm, (size_t)nraw, s))) break;
-        if (nraw > 0) make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(
-            raw_in, nraw, skey);
-        if ((st = bucket_sort(raw_out, skey, nraw, n_out, bucket_ptr, perm, flags, s))) break;
+        if (nraw > 0)
+            make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(raw_in, nraw, skey);
+        if ((st = bucket_sort(raw_out, skey, nraw, n_out_all, bucket_ptr, perm, flags, s))) break;
         dfree(skey, s);
         skey = nullptr;
         if ((st = dalloc(&tmp_col, (size_t)nraw, s))) break;
         if ((st = dalloc(&tmp_val, (size_t)nraw, s))) break;
-        if ((st = dalloc(&row_nnz, (size_t)n_out + 1, s))) break;
-        cudaMemsetAsync(row_nnz + n_out, 0, sizeof(int64_t), s);
-        merge_rows<<<grid_for(n_out, 128), 128, 0, s>>>(bucket_ptr, perm, raw_in, raw_val, n_out, tmp_col,
-                                                        tmp_val, row_nnz);
-        if ((st = dalloc(&W->row_ptr, (size_t)n_out + 1, s))) break;
-        if ((st = exclusive_scan_i64(row_nnz, W->row_ptr, n_out + 1, total_dev, s))) break;
-        int64_t nnz = 0;
-        cudaMemcpyAsync(&nnz, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        if ((st = dalloc(&row_nnz, (size_t)n_out_all + 1, s))) break;
+        cudaMemsetAsync(row_nnz + n_out_all, 0, sizeof(int64_t), s);
+        merge_rows<<<grid_for(n_out_all, 128), 128, 0, s>>>(bucket_ptr, perm, raw_in, raw_val, n_out_all, tmp_col,
+                                                            tmp_val, row_nnz);
+        if ((st = dalloc(&row_ptr, (size_t)n_out_all + 1, s))) break;
+        if ((st = exclusive_scan_i64(row_nnz, row_ptr, n_out_all + 1, total_dev, s))) break;
+        if ((st = dalloc(&nnz_base_dev, (size_t)G + 1, s))) break;
+        nnz_bases<<<grid_for(G + 1, 128), 128, 0, s>>>(row_ptr, out_base_dev, G, nnz_base_dev);
+        std::vector<int64_t> nnz_base((size_t)G + 1, 0);
+        cudaMemcpyAsync(nnz_base.data(), nnz_base_dev, sizeof(int64_t) * (G + 1), cudaMemcpyDeviceToHost, s);
+        std::vector<unsigned> fl2((size_t)G, 0u);
+        cudaMemcpyAsync(fl2.data(), flags, sizeof(unsigned) * G, cudaMemcpyDeviceToHost, s);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
-            set_error("build_conservative_2d (merge): %s", cudaGetErrorString(e));
+            set_error("conservative build (merge): %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
             break;
         }
-        if (fl & FLAG_CAPACITY) {
-            set_error("conservative sweep: the write walk disagreed with the count walk");
-            st = RG_ERR_WALK;
-            break;
-        }
-        if ((st = dalloc(&W->col, (size_t)nnz, s))) break;
-        if ((st = dalloc(&W->val, (size_t)nnz, s))) break;
-        compact_rows<<<grid_for(n_out, 128), 128, 0, s>>>(bucket_ptr, W->row_ptr, tmp_col, tmp_val, n_out,
-                                                          W->col, W->val);
+        for (int g = 0; g < G; g++)
+            if (status[g] == RG_OK && (fl2[g] & FLAG_CAPACITY)) {
+                set_error("conservative sweep: the write walk disagreed with the count walk");
+                status[g] = RG_ERR_WALK;
+            }
+        const int64_t nnz = nnz_base[G];
+        if ((st = dalloc(&col, (size_t)nnz, s))) break;
+        if ((st = dalloc(&val, (size_t)nnz, s))) break;
+        compact_rows<<<grid_for(n_out_all, 128), 128, 0, s>>>(bucket_ptr, row_ptr, tmp_col, tmp_val, n_out_all, col,
+                                                              val);
         e = cudaGetLastError();
         if (e != cudaSuccess) {
-            set_error("build_conservative_2d: %s", cudaGetErrorString(e));
+            set_error("conservative build: %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
             break;
         }
-        W->n_in = n_in;
-        W->n_out = n_out;
-        W->nnz = nnz;
-        W->out_shape0 = ncx_out;
-        W->out_shape1 = ncy_out;
-        W->in_shape0 = ncx_in;
-        W->in_shape1 = ncy_in;
+
+        // hand every grid its CSR: a single pair takes the arrays as they
+        // are, several get their own copies (no synchronisation)
+        auto fill_handle = [&](int g) {
+            const PairSpec& q = pairs[g];
+            W[g]->n_in = in_base[g + 1] - in_base[g];
+            W[g]->n_out = out_base[g + 1] - out_base[g];
+            W[g]->nnz = nnz_base[g + 1] - nnz_base[g];
+            W[g]->out_shape0 = q.nxo - 1;
+            W[g]->out_shape1 = q.nyo - 1;
+            W[g]->in_shape0 = q.nxi - 1;
+            W[g]->in_shape1 = q.nyi - 1;
+        };
+        if (G == 1) {
+            W[0]->row_ptr = row_ptr;
+            W[0]->col = col;
+            W[0]->val = val;
+            fill_handle(0);
+            row_ptr = nullptr;
+            col = nullptr;
+            val = nullptr;
+            break;
+        }
+        std::vector<void*> dst((size_t)3 * G, nullptr);
+        for (int g = 0; g < G && st == RG_OK; g++) {
+            if (status[g] != RG_OK) continue;
+            fill_handle(g);
+            if ((st = dalloc(&W[g]->row_ptr, (size_t)W[g]->n_out + 1, s))) break;
+            if ((st = dalloc(&W[g]->col, (size_t)W[g]->nnz, s))) break;
+            if ((st = dalloc(&W[g]->val, (size_t)W[g]->nnz, s))) break;
+            dst[g] = W[g]->row_ptr;
+            dst[G + g] = W[g]->col;
+            dst[2 * G + g] = W[g]->val;
+        }
+        if (st) break;
+        // grids that failed get scratch destinations: their rows are copied and dropped
+        int64_t max_rows = 0, max_nnz = 0;
+        for (int g = 0; g < G; g++)
+            if (dst[g] == nullptr) {
+                max_rows = std::max(max_rows, out_base[g + 1] - out_base[g] + 1);
+                max_nnz = std::max(max_nnz, nnz_base[g + 1] - nnz_base[g]);
+            }
+        int64_t* junk_rows = nullptr;
+        int32_t* junk_col = nullptr;
+        double* junk_val = nullptr;
+        if (max_rows > 0) {
+            if ((st = dalloc(&junk_rows, (size_t)max_rows, s))) break;
+            if ((st = dalloc(&junk_col, (size_t)std::max<int64_t>(max_nnz, 1), s))) break;
+            if ((st = dalloc(&junk_val, (size_t)std::max<int64_t>(max_nnz, 1), s))) break;
+            for (int g = 0; g < G; g++)
+                if (dst[g] == nullptr) {
+                    dst[g] = junk_rows;
+                    dst[G + g] = junk_col;
+                    dst[2 * G + g] = junk_val;
+                }
+        }
+        if ((st = upload(&dst_dev, dst, s))) break;
+        split_rows<<<grid_for(n_out_all, 256) > 8192 ? 8192 : grid_for(n_out_all, 256), 256, 0, s>>>(
+            row_ptr, out_base_dev, nnz_base_dev, G, (int64_t* const*)dst_dev);
+        if (nnz > 0)
+            split_entries<<<grid_for(nnz, 256) > 8192 ? 8192 : grid_for(nnz, 256), 256, 0, s>>>(
+                col, val, nnz_base_dev, G, (int32_t* const*)(dst_dev + G), (double* const*)(dst_dev + 2 * G));
+        dfree(junk_rows, s);
+        dfree(junk_col, s);
+        dfree(junk_val, s);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("conservative build (split): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
     } while (0);
 
     dfree(area_in, s);
     dfree(bbox_d, s);
     dfree(bbox_part, s);
-    for (int k = 0; k < 2; k++) {
-        dfree(edges[k], s);
-        dfree(bptr[k], s);
-        dfree(bitems[k], s);
-    }
+    for (auto& r : prep) free_static(&r, s);
+    dfree(totals, s);
+    dfree(P_dev, s);
+    dfree(line_base_dev, s);
+    dfree(out_base_dev, s);
+    dfree(chunk_base_dev, s);
+    dfree(plans_dev, s);
     dfree(seats, s);
     dfree(total_dev, s);
     dfree(flags, s);
@@ -1410,7 +1666,29 @@ int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64
     dfree(tmp_col, s);
     dfree(tmp_val, s);
     dfree(row_nnz, s);
+    dfree(row_ptr, s);
+    dfree(col, s);
+    dfree(val, s);
+    dfree(nnz_base_dev, s);
+    dfree(dst_dev, s);
     return st;
 }
 
+int build_conservative_2d(const double* xi, const double* yi, int64_t nxi, int64_t nyi,
+                          const double* xo, const double* yo, int64_t nxo, int64_t nyo,
+                          const double* w_in, cudaStream_t s, rg_weights_s* W) {
+    PairSpec q{xi, yi, nxi, nyi, xo, yo, nxo, nyo, w_in};
+    int status = RG_OK;
+    RG_TRY(build_batch(&q, 1, s, &W, &status));
+    return status;
+}
+
 }  // namespace rg
+
+extern "C" int rg_set_sweep_chunk(int64_t segments) {
+    RG_CHECK(segments >= 0 && segments <= (1 << 20), RG_ERR_ARG, "rg_set_sweep_chunk: %lld out of range",
+             (long long)segments);
+    rg::g_sweep_chunk.store(segments);
+    return RG_OK;
+}
+

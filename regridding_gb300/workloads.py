@@ -135,3 +135,15 @@ def served_stream(n_requests: int, rate: float = 500.0, n_cached: int = 32, reus
             reqs.append({"t": t, "pair": grid_pair(rng, log_uniform_side(rng, side_lo, side_hi)), "cached": -1,
                          "stack": stack})
     return cached, reqs
+
+
+def batched_pairs(n: int = 256, side_lo: int = 64, side_hi: int = 1024, seed: int = 3):
+    """The batched configuration: ``n`` grid pairs (``grid_pair``) with sides
+    log-uniform in [side_lo, side_hi] cells, and per pair a stack depth drawn
+    from {1, 4, 16}.  Returns (pairs, stacks)."""
+    rng = np.random.default_rng(seed)
+    pairs, stacks = [], []
+    for _ in range(n):
+        pairs.append(grid_pair(rng, log_uniform_side(rng, side_lo, side_hi)))
+        stacks.append(int(rng.choice((1, 4, 16))))
+    return pairs, stacks

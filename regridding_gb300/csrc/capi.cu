@@ -1,5 +1,6 @@
 // extern "C" entry points of libregrid_gb300 (declared in include/regrid_gb300.h).
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <new>
 #include <thread>
@@ -173,6 +174,7 @@ void init_pool_once() {
         cudaMemPool_t pool;
         if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
             uint64_t keep = POOL_KEEP_BYTES;
+            if (const char* env = getenv("RG_POOL_KEEP_BYTES")) keep = strtoull(env, nullptr, 10);
             cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &keep);
         }
         cudaGetLastError();

@@ -72,8 +72,9 @@ constexpr int64_t MAXSIZE = INT64_MAX;  // sys.maxsize: the upstream out-of-grid
 // device's default pool instead of returning it to the driver at every
 // synchronisation (the pool is this process's; the setting ends with it).
 // Builds allocate and free their scratch every call; without it each build
-// maps its scratch anew.  Implemented in capi.cu; once per device.
-constexpr uint64_t POOL_KEEP_BYTES = 8ull << 30;
+// maps its scratch anew.  RG_POOL_KEEP_BYTES overrides.  Implemented in
+// capi.cu; once per device.
+constexpr uint64_t POOL_KEEP_BYTES = 32ull << 30;
 void init_pool_once();
 
 // simple RAII-free device buffer helpers (stream ordered)

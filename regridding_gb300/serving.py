@@ -209,6 +209,7 @@ class _Job:
     weights: object = None
     slot: int = -1
     t_start: float = 0.0
+    cobuild: list = None  # one waiting request per other grid built in the same batched build
 
 
 class GpuBackend:
@@ -270,6 +271,22 @@ class GpuBackend:
             # room for the float32 weights and tile lists the first apply makes
             return dw, nbytes.value + dw.nnz * 6 + (dw.n_out // 32 + 1) * 16
 
+    def build_many(self, slot, reqs: list) -> list:
+        """Weights of several grid pairs in one batched build: per request
+        (weights, device bytes) or the exception of its failed build."""
+        pairs = [self.grids(r.grid_input, r.grid_output) for r in reqs]
+        with self.torch.cuda.stream(slot):
+            built = _device.build_conservative_2d_batch(pairs)
+        out = []
+        for dw in built:
+            if isinstance(dw, Exception):
+                out.append(dw)
+                continue
+            nbytes = ctypes.c_int64()
+            _lib.call("rg_weights_device_bytes", dw.handle, ctypes.byref(nbytes))
+            out.append((dw, nbytes.value + dw.nnz * 6 + (dw.n_out // 32 + 1) * 16))
+        return out
+
     def run(self, slot, weights, requests: list) -> None:
         t = self.torch
         with t.cuda.stream(slot):
@@ -322,11 +339,17 @@ class RegridServer:
         The upstream's default output-coordinate jitter before a build.
     intake_threads:
         Threads that hash the grids of requests submitted without a key.
+    max_cobuild:
+        A job that builds weights also builds those of up to this many other
+        waiting grids in the same batched build (their requests then find the
+        weights cached).  Off by default: on the mixed stream the slots'
+        separate builds already overlap on the GPU, and a batched build makes
+        the requests of all its grids wait for the largest.
     """
 
     def __init__(self, hbm_budget: float = 80e9, slots: int = 4, cache_bytes: float | None = None,
                  max_batch_stack: int = 64, accumulate: str = "fast", perturb: bool = True, seed: int = 42,
-                 intake_threads: int = 4, backend=None):
+                 intake_threads: int = 4, max_cobuild: int = 0, backend=None):
         if accumulate not in ("fast", "exact"):
             raise ValueError(f"accumulate must be 'fast' or 'exact', got {accumulate!r}")
         self.backend = backend if backend is not None else GpuBackend(accumulate, perturb, seed)
@@ -335,6 +358,7 @@ class RegridServer:
         self.cache = WeightsLRU(int(cache_bytes if cache_bytes is not None else hbm_budget // 2),
                                 free=self.backend.free)
         self.max_batch_stack = int(max_batch_stack)
+        self.max_cobuild = int(max_cobuild) if hasattr(self.backend, "build_many") else 0
         self._cv = threading.Condition()
         self._pending: collections.deque[_Request] = collections.deque()
         self._building: set = set()
@@ -475,6 +499,8 @@ class RegridServer:
             self.n_batches += 1
             if job.build:
                 self._building.add(job.key)
+                for r in job.cobuild or ():
+                    self._building.add(r.key)
             progressed = True
             self._cv.notify_all()
         return progressed
@@ -513,7 +539,23 @@ class RegridServer:
             for r in group:
                 self._pending.remove(r)
             weights = self.cache.acquire(head.key) if cached else None
-            return _Job(head.key, group, not cached, footprint, weights)
+            job = _Job(head.key, group, not cached, footprint, weights)
+            if not cached and self.max_cobuild > 0:
+                # other grids waiting for weights go into the same batched build
+                seen = {head.key}
+                job.cobuild = []
+                for r in self._pending:
+                    if len(job.cobuild) >= self.max_cobuild:
+                        break
+                    if r.key in seen or r.key in self.cache or r.key in self._building:
+                        continue
+                    extra = self.backend.build_bytes(r)
+                    if self._in_use() + job.footprint + extra > self.budget:
+                        break
+                    seen.add(r.key)
+                    job.cobuild.append(r)
+                    job.footprint += extra
+            return job
         return None
 
     # -- slots --------------------------------------------------------------
@@ -533,20 +575,37 @@ class RegridServer:
         job.t_start = time.perf_counter()
         err = None
         built = False
+        cobuild = job.cobuild or []
         try:
             if job.build:
-                weights, nbytes = self.backend.build(stream, job.requests[0])
+                if cobuild:
+                    results = self.backend.build_many(stream, [job.requests[0]] + cobuild)
+                else:
+                    results = [self.backend.build(stream, job.requests[0])]
                 with self._cv:
-                    self.cache.insert(job.key, weights, nbytes)
-                    self._building.discard(job.key)
-                    # the build scratch is returned; the weights now count in the cache
-                    scratch = self.backend.build_bytes(job.requests[0])
-                    self._transient -= scratch
-                    job.footprint -= scratch
+                    for req, res in zip([job.requests[0]] + cobuild, results):
+                        head = req is job.requests[0]
+                        self._building.discard(req.key)
+                        if isinstance(res, Exception):
+                            if not head:
+                                # the requests of a grid whose build failed fail with it
+                                for r in [r for r in self._pending if r.key == req.key]:
+                                    self._pending.remove(r)
+                                    r.future.set_exception(res)
+                            continue
+                        self.cache.insert(req.key, res[0], res[1])
+                        if not head:
+                            self.cache.release(req.key)  # no job holds it yet
+                        # the build scratch is returned; the weights now count in the cache
+                        scratch = self.backend.build_bytes(req)
+                        self._transient -= scratch
+                        job.footprint -= scratch
+                        self.n_builds += 1
                     self.peak_bytes = max(self.peak_bytes, self._in_use())
-                    self.n_builds += 1
                     self._cv.notify_all()
-                job.weights = weights
+                if isinstance(results[0], Exception):
+                    raise results[0]
+                job.weights = results[0][0]
                 built = True
             self.backend.run(stream, job.weights, job.requests)
         except Exception as e:  # noqa: BLE001 - reported through the futures
@@ -555,6 +614,8 @@ class RegridServer:
         with self._cv:
             if job.build and not built:
                 self._building.discard(job.key)
+                for r in cobuild:
+                    self._building.discard(r.key)
             if job.weights is not None or built:
                 self.cache.release(job.key)
             self._transient -= job.footprint

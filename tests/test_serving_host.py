@@ -207,3 +207,45 @@ def test_unkeyed_requests_are_hashed_and_batched_by_grid():
     srv.close()  # waits for the keying pool, then drains
     assert all(f.exception() is None for f in fs)
     assert len(set(be.builds)) == 2 and len(be.builds) == 2
+
+
+class FakeBatchBackend(FakeBackend):
+    def __init__(self, **kw):
+        super().__init__(**kw)
+        self.build_calls = []
+
+    def build_many(self, slot, reqs):
+        with self.lock:
+            self.build_calls.append([r.key for r in reqs])
+        out = []
+        for r in reqs:
+            try:
+                out.append(self.build(slot, r))
+            except Exception as e:  # noqa: BLE001
+                out.append(e)
+        return out
+
+
+def test_cobuilds_share_one_batched_build():
+    """While a slot is busy, requests for several new grids wait; the next
+    job builds all their weights in one batched build, later jobs find them
+    cached, and a grid whose build fails fails only its own requests."""
+    gate = threading.Event()
+    be = FakeBatchBackend(gate=gate, fail_build={"k3"})
+    gi, go = grids(3, 2)
+    with RegridServer(hbm_budget=10**9, slots=1, backend=be, max_cobuild=8) as srv:
+        first = srv.submit(gi, go, np.ones((1, 3, 3)), key="k0")  # holds the slot
+        time.sleep(0.1)
+        fs = {k: srv.submit(gi, go, np.ones((1, 3, 3)), key=k) for k in ("k1", "k2", "k3", "k4")}
+        time.sleep(0.1)
+        gate.set()
+        first.result(5)
+        for k, f in fs.items():
+            if k == "k3":
+                with pytest.raises(RuntimeError, match="build failed"):
+                    f.result(5)
+            else:
+                np.testing.assert_array_equal(f.result(5), np.ones((1, 9)) @ FakeBackend.matrix(k, 9, 4).T)
+        st = srv.stats()
+    assert ["k1", "k2", "k3", "k4"] in be.build_calls  # one batched build for the four waiting grids
+    assert st["builds"] == 4  # k0, k1, k2, k4

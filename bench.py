@@ -252,7 +252,8 @@ def run_serving(args, torch):
     for mode in ("poisson", "saturated"):
         # a fresh server per pass: the 32 resident grids are built before the
         # stream starts, every new grid of the stream is built during it
-        with RegridServer(hbm_budget=80e9, slots=args.serve_slots, max_batch_stack=64, perturb=False) as srv:
+        with RegridServer(hbm_budget=80e9, slots=args.serve_slots, max_batch_stack=64, perturb=False,
+                          max_cobuild=args.serve_cobuild) as srv:
             warm = [srv.submit(gi, go, np.zeros((1, cells(gi)), np.float32)) for gi, go in cached]
             for f in warm:
                 f.result()
@@ -398,6 +399,51 @@ def run_batched(args, torch):
             "build_speedup": round(t_single / t_batch, 2),
             "apply_graph_ms": round(t_graph * 1e3, 3), "apply_eager_ms": round(t_eager * 1e3, 3),
             "apply_graph_GB_per_s": round(nbytes / t_graph / 1e9, 1)}
+
+
+def run_multilinear_1d(args, torch):
+    """The 1D case of the 2048^2 configuration: multilinear weights from a
+    shared non-uniform sorted axis of 4096 samples (sorted uniform(0, 1)) to
+    4096 sorted output points, applied to 10^6 float32 spectra (16.4 GB in,
+    16.4 GB out, resident in HBM); the CPU oracle applies the same weights
+    to a 10^4-spectrum sample."""
+    import oracle
+    import regridding_gb300 as rg
+    from regridding_gb300 import _device
+
+    rng = np.random.default_rng(12)
+    x_in = np.sort(rng.uniform(0, 1, 4096))
+    x_out = np.sort(rng.uniform(x_in[0], x_in[-1], 4096))
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    w, shape_in, shape_out = rg.weights(x_in, x_out, method="multilinear")
+    t_w = time.perf_counter() - t0
+    ii, oo, vv = w[()] if w.shape == () else w.reshape(-1)[0]
+    dw = _device.DeviceWeights.from_coo(ii, oo, vv, 4096, 4096)
+    n_spec = 1_000_000
+    g = torch.Generator(device="cuda")
+    g.manual_seed(13)
+    vals = torch.rand((n_spec, 4096), generator=g, device="cuda", dtype=torch.float32)
+    out = torch.empty((n_spec, 4096), dtype=torch.float32, device="cuda")
+    per, wall = time_launches(lambda: dw.apply(vals, out=out, accumulate="fast"), 5, 3, torch.cuda.current_stream(),
+                              torch)
+    nbytes = apply_bytes(n_spec, 4096, 4096, dw.nnz)
+    # parity on a sample of spectra against the oracle's float64 apply
+    sample = vals[:2048].cpu().numpy()
+    exp = oracle.apply(ii, oo, vv, sample.astype(np.float64), 4096)
+    rel = float(np.max(np.abs(out[:2048].cpu().numpy() - exp) / np.maximum(np.abs(exp), 1e-30)))
+    # CPU oracle on 10^4 spectra
+    host = vals[:10_000].cpu().numpy()
+    t0 = time.perf_counter()
+    oracle.apply(ii, oo, vv, host, 4096)
+    t_cpu = time.perf_counter() - t0
+    del vals, out
+    return {"workload": "1D multilinear, 4096 -> 4096 samples, 10^6 float32 spectra", "nnz": int(dw.nnz),
+            "weights_ms": round(t_w * 1e3, 2), "apply_ms": round(statistics.mean(per) * 1e3, 3),
+            "apply_GB_per_s": round(nbytes / statistics.mean(per) / 1e9, 1),
+            "spectra_per_s": round(n_spec / statistics.mean(per), 0), "max_rel_err_vs_f64_sample": rel,
+            "cpu_baseline": {"spectra_per_s": round(10_000 / t_cpu, 0), "cores": os.cpu_count(),
+                             "kind": "port", "sample": "10^4 spectra, float64 output"}}
 
 
 def run_differentiable(args, torch):
@@ -613,6 +659,7 @@ def run_ours(args, world, rank, local):
     if rank == 0 and args.serve_requests > 0:
         line["serving"] = run_serving(args, torch)
     if rank == 0 and not args.no_extra:
+        line["multilinear_1d"] = run_multilinear_1d(args, torch)
         line["batched"] = run_batched(args, torch)
         line["differentiable"] = run_differentiable(args, torch)
     if rank == 0:
@@ -696,6 +743,7 @@ def main(argv=None):
     p.add_argument("--stack", type=int, default=STACK)
     p.add_argument("--serve-requests", type=int, default=1000, help="requests of the served stream (0: skip)")
     p.add_argument("--serve-slots", type=int, default=16)
+    p.add_argument("--serve-cobuild", type=int, default=0, help="small grids built together per build job")
     p.add_argument("--no-extra", action="store_true", help="skip the differentiable-regrid and batched legs")
     args = p.parse_args(argv)
     if args.warmup < 3:

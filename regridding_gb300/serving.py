@@ -339,17 +339,19 @@ class RegridServer:
         The upstream's default output-coordinate jitter before a build.
     intake_threads:
         Threads that hash the grids of requests submitted without a key.
-    max_cobuild:
-        A job that builds weights also builds those of up to this many other
-        waiting grids in the same batched build (their requests then find the
-        weights cached).  Off by default: on the mixed stream the slots'
-        separate builds already overlap on the GPU, and a batched build makes
-        the requests of all its grids wait for the largest.
+    max_cobuild, cobuild_max_cells:
+        A job that builds the weights of a small grid pair (at most
+        ``cobuild_max_cells`` input cells) also builds those of up to
+        ``max_cobuild`` other small waiting pairs in the same batched build
+        (their requests then find the weights cached).  Small builds are
+        dominated by fixed per-build costs that a batch pays once; large
+        builds gain little and would make the small ones wait.
     """
 
     def __init__(self, hbm_budget: float = 80e9, slots: int = 4, cache_bytes: float | None = None,
                  max_batch_stack: int = 64, accumulate: str = "fast", perturb: bool = True, seed: int = 42,
-                 intake_threads: int = 4, max_cobuild: int = 0, backend=None):
+                 intake_threads: int = 4, max_cobuild: int = 0, cobuild_max_cells: int = 512 * 512,
+                 backend=None):
         if accumulate not in ("fast", "exact"):
             raise ValueError(f"accumulate must be 'fast' or 'exact', got {accumulate!r}")
         self.backend = backend if backend is not None else GpuBackend(accumulate, perturb, seed)
@@ -359,6 +361,7 @@ class RegridServer:
                                 free=self.backend.free)
         self.max_batch_stack = int(max_batch_stack)
         self.max_cobuild = int(max_cobuild) if hasattr(self.backend, "build_many") else 0
+        self.cobuild_max_cells = int(cobuild_max_cells)
         self._cv = threading.Condition()
         self._pending: collections.deque[_Request] = collections.deque()
         self._building: set = set()
@@ -540,14 +543,16 @@ class RegridServer:
                 self._pending.remove(r)
             weights = self.cache.acquire(head.key) if cached else None
             job = _Job(head.key, group, not cached, footprint, weights)
-            if not cached and self.max_cobuild > 0:
-                # other grids waiting for weights go into the same batched build
+            if not cached and self.max_cobuild > 0 and head.n_in <= self.cobuild_max_cells:
+                # other small grids waiting for weights go into the same batched build
                 seen = {head.key}
                 job.cobuild = []
                 for r in self._pending:
                     if len(job.cobuild) >= self.max_cobuild:
                         break
                     if r.key in seen or r.key in self.cache or r.key in self._building:
+                        continue
+                    if r.n_in > self.cobuild_max_cells:
                         continue
                     extra = self.backend.build_bytes(r)
                     if self._in_use() + job.footprint + extra > self.budget:

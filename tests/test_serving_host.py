@@ -233,7 +233,7 @@ def test_cobuilds_share_one_batched_build():
     gate = threading.Event()
     be = FakeBatchBackend(gate=gate, fail_build={"k3"})
     gi, go = grids(3, 2)
-    with RegridServer(hbm_budget=10**9, slots=1, backend=be, max_cobuild=8) as srv:
+    with RegridServer(hbm_budget=10**9, slots=1, backend=be, max_cobuild=8, cobuild_max_cells=100) as srv:
         first = srv.submit(gi, go, np.ones((1, 3, 3)), key="k0")  # holds the slot
         time.sleep(0.1)
         fs = {k: srv.submit(gi, go, np.ones((1, 3, 3)), key=k) for k in ("k1", "k2", "k3", "k4")}

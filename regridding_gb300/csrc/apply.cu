@@ -168,6 +168,8 @@ bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack);
 int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made);
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int rows_usable(rg_weights_s* W, const float* vin, int64_t stack, cudaStream_t s, bool* made, bool* ok);
+int apply_rows_launch(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int ensure_transposed(rg_weights_s* W, cudaStream_t s);
 
 // Every apply goes through here.  The per-handle state an apply needs beyond
@@ -187,7 +189,7 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
                        W->n_out > 0 && W->nnz > 0;
     const bool need32 = acc == RG_ACC_FAST && dtype_out == RG_F32 && W->nnz > 0;
     int g = 0;
-    bool use_box = false;
+    bool use_box = false, use_rows = false;
     {
         std::lock_guard<std::mutex> lock(W->mu);
         bool made = false;
@@ -212,9 +214,11 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
             }
             use_box = use_box && W->box_cfg >= 0;
         }
-        if (tiled && !use_box) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
+        if (tiled && !use_box) RG_TRY(rows_usable(W, (const float*)vin, stack, s, &made, &use_rows));
+        if (tiled && !use_box && !use_rows) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
         if (made) RG_CUDA(cudaStreamSynchronize(s));
     }
+    if (use_rows) return apply_rows_launch(W, (const float*)vin, (float*)vout, stack, s);
     if (use_box) {
         const int st = apply_box(W, (const float*)vin, (float*)vout, stack, s);
         if (st != RG_ERR_UNSUPPORTED) return st;

@@ -601,6 +601,117 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Row variant, for weights with a short input axis (a whole slice fits in
+// shared memory: 1D multilinear or conservative weights over many spectra).
+// A persistent block of ROWS_THREADS threads walks slices d = blockIdx.x,
+// blockIdx.x + gridDim.x, ...; thread 0 fills a ring of ROWS_NST stages with
+// one 1D bulk copy per slice (cp.async.bulk, completed by the stage's full
+// mbarrier); every thread keeps the entries of its outputs (o = t, t + T,
+// ...; at most ROWS_E entries each) in registers, reduces them from shared
+// memory and stores coalesced; warps release a stage on its empty mbarrier.
+// ---------------------------------------------------------------------------
+
+constexpr int ROWS_THREADS = 1024;
+constexpr int ROWS_J = 4;   // outputs per thread (n_out <= ROWS_THREADS * ROWS_J)
+constexpr int ROWS_E = 4;   // entries per output at most
+constexpr int ROWS_NST = 3;
+
+__device__ __forceinline__ void bulk_load(float* dst, const float* src, unsigned bytes, uint64_t* bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+            smem_u32(dst)),
+        "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__global__ void __launch_bounds__(ROWS_THREADS, 1)
+    apply_rows(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, const float* __restrict__ val,
+               const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout, int64_t n_out, int64_t stack,
+               int stage_floats, unsigned* __restrict__ flags) {
+    __shared__ __align__(8) uint64_t full[ROWS_NST], empty[ROWS_NST];
+    extern __shared__ __align__(128) float rbuf[];
+    const int t = threadIdx.x, lane = t & 31;
+    constexpr int NWARPS = ROWS_THREADS / 32;
+    int c[ROWS_J][ROWS_E];
+    float w[ROWS_J][ROWS_E];
+#pragma unroll
+    for (int j = 0; j < ROWS_J; j++) {
+        const int64_t o = t + (int64_t)j * ROWS_THREADS;
+        int64_t s = 0, e = 0;
+        if (o < n_out) {
+            s = row_ptr[o];
+            e = row_ptr[o + 1];
+        }
+#pragma unroll
+        for (int k = 0; k < ROWS_E; k++) {
+            c[j][k] = s + k < e ? col[s + k] : 0;
+            w[j][k] = s + k < e ? val[s + k] : 0.f;
+        }
+    }
+    if (t == 0) {
+        for (int k = 0; k < ROWS_NST; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], NWARPS);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    __syncthreads();
+    const unsigned bytes = (unsigned)(n_in * 4);
+    // slices of this block: d = blockIdx.x + i * gridDim.x
+    const int64_t nmine = blockIdx.x < stack ? (stack - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    auto issue = [&](int st, int64_t i) {
+        mbar_expect_tx(&full[st], bytes);
+        bulk_load(rbuf + (int64_t)st * stage_floats, vin + (blockIdx.x + i * gridDim.x) * n_in, bytes, &full[st]);
+    };
+    if (t == 0)
+        for (int k = 0; k < ROWS_NST && k < nmine; k++) issue(k, k);
+    for (int64_t i = 0; i < nmine; i++) {
+        const int st = (int)(i % ROWS_NST);
+        const unsigned ph = (unsigned)((i / ROWS_NST) & 1);
+        const bool got = mbar_wait_bounded(&full[st], ph);
+        if (!__all_sync(0xffffffffu, got)) {
+            if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
+            if (t == 0)
+                for (int64_t q = i + 1; q < i + ROWS_NST && q < nmine; q++)
+                    (void)mbar_wait_bounded(&full[q % ROWS_NST], (unsigned)((q / ROWS_NST) & 1));
+            return;
+        }
+        const float* buf = rbuf + (int64_t)st * stage_floats;
+        float* out = vout + (blockIdx.x + i * gridDim.x) * n_out;
+#pragma unroll
+        for (int j = 0; j < ROWS_J; j++) {
+            const int64_t o = t + (int64_t)j * ROWS_THREADS;
+            if (o < n_out) {
+                float acc = 0.f;
+#pragma unroll
+                for (int k = 0; k < ROWS_E; k++) acc = fmaf(w[j][k], buf[c[j][k]], acc);
+                out[o] = acc;
+            }
+        }
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[st]);
+        if (t == 0 && i + ROWS_NST < nmine) {
+            if (!mbar_wait_bounded(&empty[st], ph)) {
+                atomicOr(flags, FLAG_TIMEOUT);
+                for (int64_t q = i + 1; q < i + ROWS_NST && q < nmine; q++)
+                    (void)mbar_wait_bounded(&full[q % ROWS_NST], (unsigned)((q / ROWS_NST) & 1));
+                return;
+            }
+            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+            issue(st, i + ROWS_NST);
+        }
+    }
+}
+
+// longest row of a CSR (atomicMax over rows)
+__global__ void max_row_len(const int64_t* __restrict__ row_ptr, int64_t n, unsigned* __restrict__ out) {
+    for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n; o += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t len = row_ptr[o + 1] - row_ptr[o];
+        atomicMax(out, (unsigned)(len > 0xffffffffll ? 0xffffffffll : len));
+    }
+}
+
 typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
                                   const cuuint64_t*, const cuuint32_t*, const cuuint32_t*, CUtensorMapInterleave,
                                   CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
@@ -1061,6 +1172,55 @@ int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cuda
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
     if (W->box_cfg < 0) return RG_ERR_UNSUPPORTED;
     return launch_box_config(W, W->box_cfg, vin, vout, stack, s);
+}
+
+// Whether the row kernel can take this call (the caller holds the lock and
+// has made val32): a whole input slice fits a stage, every output fits a
+// thread's registers, and the stack is long enough to fill the GPU.
+// Builds the handle's row facts on first use (*made set).
+int rows_usable(rg_weights_s* W, const float* vin, int64_t stack, cudaStream_t s, bool* made, bool* ok) {
+    *ok = false;
+    if (W->n_in % 4 != 0 || W->n_in > 12288 || W->n_out > (int64_t)ROWS_THREADS * ROWS_J || W->n_in >= INT32_MAX ||
+        ((uintptr_t)vin & 15) != 0 || stack < 2 * 152)
+        return RG_OK;
+    if (W->rows_maxlen < 0) {
+        unsigned* d = nullptr;
+        RG_TRY(dalloc(&d, 1, s));
+        cudaMemsetAsync(d, 0, sizeof(unsigned), s);
+        max_row_len<<<grid_for(W->n_out, 256) > 1024 ? 1024 : grid_for(W->n_out, 256), 256, 0, s>>>(W->row_ptr,
+                                                                                                   W->n_out, d);
+        unsigned h = 0;
+        cudaMemcpyAsync(&h, d, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        cudaError_t e = cudaStreamSynchronize(s);
+        dfree(d, s);
+        if (e != cudaSuccess) {
+            set_error("apply (row facts): %s", cudaGetErrorString(e));
+            return RG_ERR_CUDA;
+        }
+        W->rows_maxlen = (int)std::min<unsigned>(h, 1u << 30);
+        if (W->dflags == nullptr) {
+            RG_TRY(dalloc(&W->dflags, 1, s));
+            cudaMemsetAsync(W->dflags, 0, sizeof(unsigned), s);
+            *made = true;
+        }
+    }
+    *ok = W->rows_maxlen <= ROWS_E;
+    return RG_OK;
+}
+
+int apply_rows_launch(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+    const int stage_floats = (int)((W->n_in + 31) & ~31ll);  // stages start on 128-byte boundaries
+    const size_t smem = (size_t)ROWS_NST * stage_floats * sizeof(float);
+    static std::once_flag attr;
+    std::call_once(attr, []() {
+        cudaFuncSetAttribute(apply_rows, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        cudaGetLastError();
+    });
+    const int64_t blocks = std::min<int64_t>(stack, 152 * 2);
+    apply_rows<<<(unsigned)blocks, ROWS_THREADS, smem, s>>>(W->row_ptr, W->col, W->val32, vin, W->n_in, vout,
+                                                            W->n_out, stack, stage_floats, W->dflags);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
 }
 
 }  // namespace rg

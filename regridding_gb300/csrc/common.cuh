@@ -157,6 +157,7 @@ struct rg_weights_s {
     uint16_t* box_slot = nullptr;  // per entry, in the order the TMA kernel gathers them
     float* box_val = nullptr;      // float32 weights in that order
     unsigned* dflags = nullptr;  // device error word of the asynchronous (TMA) apply
+    int rows_maxlen = -1;        // longest row (for the row kernel; -1 not known yet)
     int device = 0;
     std::mutex mu;  // guards the lazily made state above (made on first use by an apply)
 };

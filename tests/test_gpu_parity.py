@@ -609,3 +609,40 @@ def test_fast_apply_paths(rg, case, stack):
     from regridding_gb300 import _lib
 
     _lib.call("rg_weights_check", dw.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
+@pytest.mark.parametrize("kind", ["multilinear", "conservative_coarse"])
+def test_row_kernel_long_stacks(rg, kind):
+    """Weights with a short input axis over a long stack take the row kernel
+    (whole slices staged by bulk copies); its results are within the float32
+    bound of the oracle and bit-identical to the same weights over a short
+    stack (warp-staged kernel, same per-row order).  Rows longer than the
+    kernel holds (coarse conservative output) take the other kernels."""
+    import torch
+
+    from regridding_gb300._device import DeviceWeights
+
+    rng = np.random.default_rng(31)
+    x_in = np.sort(rng.uniform(0, 1, 512))
+    if kind == "multilinear":
+        x_out = np.sort(rng.uniform(x_in[0], x_in[-1], 400))
+        w, _, _ = rg.weights(x_in, x_out, method="multilinear")
+    else:
+        x_out = np.linspace(x_in[0], x_in[-1], 41)  # ~13 input cells per output cell
+        w, _, _ = rg.weights(x_in, x_out, method="conservative")
+    ii, oo, vv = w[()] if w.shape == () else w.reshape(-1)[0]
+    n_in = 512 if kind == "multilinear" else 511  # conservative: 511 cells
+    n_out = 400 if kind == "multilinear" else 40
+    dw = DeviceWeights.from_coo(ii, oo, vv, n_in, n_out)
+    vals = rng.uniform(0.5, 2.0, (700, n_in)).astype(np.float32)
+    d_vals = torch.from_numpy(vals).cuda()
+    got = dw.apply(d_vals, accumulate="fast").cpu().numpy()
+    short = dw.apply(d_vals[:37].contiguous(), accumulate="fast").cpu().numpy()
+    assert_same(short, got[:37])
+    exp = oracle.apply(ii, oo, vv, vals.astype(np.float64), n_out)
+    k = np.bincount(oo, minlength=n_out)
+    bound = (k + 2) * 2.0**-24 * oracle.apply(ii, oo, np.abs(vv), np.abs(vals).astype(np.float64), n_out)
+    assert np.all(np.abs(got - exp) <= bound)
+    from regridding_gb300 import _lib
+
+    _lib.call("rg_weights_check", dw.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))

@@ -167,6 +167,7 @@ int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int
 bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack);
 int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made);
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int apply_box_exact(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s);
 int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int rows_usable(rg_weights_s* W, const float* vin, int64_t stack, cudaStream_t s, bool* made, bool* ok);
 int apply_rows_launch(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
@@ -187,9 +188,13 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
     // tensor-map copies when the input grid shape allows, else by the warps)
     const bool tiled = !transposed && acc == RG_ACC_FAST && dtype_in == RG_F32 && dtype_out == RG_F32 &&
                        W->n_out > 0 && W->nnz > 0;
-    const bool need32 = acc == RG_ACC_FAST && dtype_out == RG_F32 && W->nnz > 0;
+    // the exact float64 apply of a float32 stack stages input boxes too
+    const bool exact_box = !transposed && acc == RG_ACC_EXACT && dtype_in == RG_F32 && dtype_out == RG_F64 &&
+                           W->n_out > 0 && W->nnz > 0;
+    // (the patch lists keep a float32 copy of the weights in gather order)
+    const bool need32 = ((acc == RG_ACC_FAST && dtype_out == RG_F32) || exact_box) && W->nnz > 0;
     int g = 0;
-    bool use_box = false, use_rows = false;
+    bool use_box = false, use_rows = false, use_box_exact = false;
     {
         std::lock_guard<std::mutex> lock(W->mu);
         bool made = false;
@@ -214,11 +219,19 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
             }
             use_box = use_box && W->box_cfg >= 0;
         }
+        if (exact_box && box_usable(W, (const float*)vin, stack)) {
+            RG_TRY(box_lists_for(W, s, &made));
+            use_box_exact = W->box_state == 1;
+        }
         if (tiled && !use_box) RG_TRY(rows_usable(W, (const float*)vin, stack, s, &made, &use_rows));
         if (tiled && !use_box && !use_rows) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
         if (made) RG_CUDA(cudaStreamSynchronize(s));
     }
     if (use_rows) return apply_rows_launch(W, (const float*)vin, (float*)vout, stack, s);
+    if (use_box_exact) {
+        const int st = apply_box_exact(W, (const float*)vin, (double*)vout, stack, s);
+        if (st != RG_ERR_UNSUPPORTED) return st;
+    }
     if (use_box) {
         const int st = apply_box(W, (const float*)vin, (float*)vout, stack, s);
         if (st != RG_ERR_UNSUPPORTED) return st;

@@ -495,11 +495,38 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
     }
 }
 
-template <int SPS, int NST, int MINB>
+// Box slot of input cell c (natural CSR order, for the exact kernel).
+__device__ __forceinline__ int box_slot_of(int c, int2 org, int64_t n1_in) {
+    const int row = (int)(c / n1_in);
+    const int r = row - org.x, cc = (int)(c - (int64_t)row * n1_in) - org.y;
+    return r * PBOX_C + ((((cc >> 2) ^ (r & 7)) << 2) | (cc & 3));
+}
+
+// float32 -> float64, exactly, on the integer pipe: for a normal binary32
+// value the binary64 value has the same sign, the exponent rebiased from 127
+// to 1023 and the 23 fraction bits followed by 29 zeros.  Zeros, subnormals,
+// infinities and NaNs take the hardware conversion.  (The exact apply spends
+// most of its FP64 issue slots on its multiply and add; this keeps the
+// conversion off that pipe.)
+__device__ __forceinline__ double widen(float f) {
+    const unsigned u = __float_as_uint(f);
+    const unsigned ex = (u >> 23) & 0xffu;
+    if (ex == 0u || ex == 0xffu) return (double)f;
+    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
+                                    ((unsigned long long)(ex + (1023u - 127u)) << 52) |
+                                    ((unsigned long long)(u & 0x7fffffu) << 29);
+    return __longlong_as_double((long long)bits);
+}
+
+// EXACT: the upstream float64 apply bit for bit (float32 input, float64
+// weights and output): every entry in stored (CSR) order as
+// acc = acc + w * (double)x with one rounding per operation, from 0.0.
+template <int SPS, int NST, int MINB, bool EXACT>
 __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     apply_patch_tma(const __grid_constant__ CUtensorMap tmap, const int64_t* __restrict__ row_ptr,
                     const int32_t* __restrict__ col, const uint16_t* __restrict__ slot,
                     const float* __restrict__ bval, const float* __restrict__ val,
+                    const double* __restrict__ dval, double* __restrict__ vout64, int64_t n1_in,
                     PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
                     unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
                     int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags) {
@@ -520,7 +547,18 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     const int2 org = origin[p];
     if (org.x < 0) {
         // no entries (all zeros) or a footprint larger than the box: the whole block
-        if (o >= 0) apply_direct(s, e, col, val, vin, n_in, out, n_out, d0, d1);
+        if (o >= 0) {
+            if constexpr (EXACT) {
+                for (int64_t d = d0; d < d1; d++) {
+                    const float* a = vin + d * n_in;
+                    double acc = 0.0;
+                    for (int64_t k = s; k < e; k++) acc = __dadd_rn(acc, __dmul_rn(dval[k], (double)__ldg(a + col[k])));
+                    vout64[d * n_out + o] = acc;
+                }
+            } else {
+                apply_direct(s, e, col, val, vin, n_in, out, n_out, d0, d1);
+            }
+        }
         return;
     }
     const int plane = BR * PBOX_C;
@@ -530,10 +568,18 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     const int flip = (BR & 4) ? 16 : 0;
     int li[CACHED_T];
     float w[CACHED_T];
+    double wd[CACHED_T];
 #pragma unroll
     for (int k = 0; k < CACHED_T; k++) {
-        li[k] = k < nk ? (int)slot[s + k] : 0;
-        w[k] = k < nk ? bval[s + k] : 0.f;
+        if constexpr (EXACT) {
+            li[k] = k < nk ? box_slot_of(col[s + k], org, n1_in) : 0;
+            wd[k] = k < nk ? dval[s + k] : 0.0;
+            w[k] = 0.f;
+        } else {
+            li[k] = k < nk ? (int)slot[s + k] : 0;
+            w[k] = k < nk ? bval[s + k] : 0.f;
+            wd[k] = 0.0;
+        }
     }
     if (t == 0) {
         for (int k = 0; k < NST; k++) {
@@ -563,7 +609,32 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
         }
         const float* buf = ring + (int64_t)st * stage_floats;
         const int64_t ds = d0 + grp * SPS;
-        if (o >= 0) {
+        if constexpr (EXACT) {
+            if (o >= 0) {
+                double acc[SPS];
+#pragma unroll
+                for (int q = 0; q < SPS; q++) acc[q] = 0.0;
+#pragma unroll
+                for (int k = 0; k < CACHED_T; k++) {
+                    if (k < nk) {
+#pragma unroll
+                        for (int q = 0; q < SPS; q++)
+                            acc[q] = __dadd_rn(
+                                acc[q], __dmul_rn(wd[k], widen(buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))])));
+                    }
+                }
+                for (int64_t k = s + CACHED_T; k < e; k++) {
+                    const double wk = dval[k];
+                    const int sk = box_slot_of(col[k], org, n1_in);
+#pragma unroll
+                    for (int q = 0; q < SPS; q++)
+                        acc[q] = __dadd_rn(acc[q], __dmul_rn(wk, widen(buf[q * plane + (sk ^ ((q & 1) ? flip : 0))])));
+                }
+#pragma unroll
+                for (int q = 0; q < SPS; q++)
+                    if (ds + q < d1) vout64[(ds + q) * n_out + o] = acc[q];
+            }
+        } else if (o >= 0) {
             float acc[SPS];
 #pragma unroll
             for (int q = 0; q < SPS; q++) acc[q] = 0.f;
@@ -1047,8 +1118,8 @@ struct BoxConfig {
 constexpr BoxConfig kBoxConfigs[] = {{4, 2, 0}, {4, 2, 4}, {4, 3, 4}, {2, 3, 4}, {2, 4, 4}, {8, 2, 0}, {4, 3, 0}};
 constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]));
 
-template <int SPS, int NST, int MINB>
-int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, const float* vin, float* vout,
+template <int SPS, int NST, int MINB, bool EXACT = false>
+int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, const float* vin, void* vout,
                  int64_t stack, cudaStream_t s) {
     const int BR = W->box_rows;
     const int stage_floats = (SPS * BR * PBOX_C + 255) & ~255;  // stages start on 1024-byte boundaries
@@ -1057,7 +1128,7 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     if (smem > 200 * 1024) return RG_ERR_UNSUPPORTED;
     static std::once_flag attr;
     std::call_once(attr, []() {
-        cudaFuncSetAttribute(apply_patch_tma<SPS, NST, MINB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(apply_patch_tma<SPS, NST, MINB, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              200 * 1024);
         cudaGetLastError();
     });
@@ -1072,11 +1143,24 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     if ((stack + chunk - 1) / chunk > 65535) chunk = ((stack + 65534) / 65535 + SPS - 1) / SPS * SPS;
     const int64_t nchunks = (stack + chunk - 1) / chunk;
     dim3 grid((unsigned)patches, (unsigned)nchunks);
-    apply_patch_tma<SPS, NST, MINB><<<grid, 32 * PATCH_WARPS, smem, s>>>(
-        map, W->row_ptr, W->col, W->box_slot, W->box_val, W->val32, patch_grid(W), patches, W->box_origin, BR,
-        stage_floats, stage_bytes, vin, W->n_in, vout, W->n_out, stack, chunk, W->dflags);
+    apply_patch_tma<SPS, NST, MINB, EXACT><<<grid, 32 * PATCH_WARPS, smem, s>>>(
+        map, W->row_ptr, W->col, W->box_slot, W->box_val, W->val32, W->val, EXACT ? (double*)vout : nullptr,
+        W->in_shape1, patch_grid(W), patches, W->box_origin, BR, stage_floats, stage_bytes, vin, W->n_in,
+        EXACT ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
+}
+
+// Tensor map of the input stack: columns x rows x slices, boxes of
+// 32 columns x box_rows x bs slices, 128-byte swizzle.
+bool encode_stack(const rg_weights_s* W, const float* vin, int64_t stack, int bs, CUtensorMap* map) {
+    const cuuint64_t dims[3] = {(cuuint64_t)W->in_shape1, (cuuint64_t)W->in_shape0, (cuuint64_t)stack};
+    const cuuint64_t strides[2] = {(cuuint64_t)W->in_shape1 * 4, (cuuint64_t)W->n_in * 4};
+    const cuuint32_t box[3] = {(cuuint32_t)PBOX_C, (cuuint32_t)W->box_rows, (cuuint32_t)bs};
+    const cuuint32_t estr[3] = {1, 1, 1};
+    return encode_tiled()(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)vin, dims, strides, box, estr,
+                          CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                          CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
@@ -1085,14 +1169,7 @@ int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* v
     // stage's other slices are never stored)
     const int bs = (int)std::min<int64_t>(c.sps, stack);
     CUtensorMap map;
-    const cuuint64_t dims[3] = {(cuuint64_t)W->in_shape1, (cuuint64_t)W->in_shape0, (cuuint64_t)stack};
-    const cuuint64_t strides[2] = {(cuuint64_t)W->in_shape1 * 4, (cuuint64_t)W->n_in * 4};
-    const cuuint32_t box[3] = {(cuuint32_t)PBOX_C, (cuuint32_t)W->box_rows, (cuuint32_t)bs};
-    const cuuint32_t estr[3] = {1, 1, 1};
-    CUresult r = encode_tiled()(&map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 3, (void*)vin, dims, strides, box, estr,
-                                CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                                CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-    if (r != CUDA_SUCCESS) return RG_ERR_UNSUPPORTED;
+    if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
         case 0: return launch_patch<4, 2, 0>(W, map, bs, vin, vout, stack, s);
         case 1: return launch_patch<4, 2, 4>(W, map, bs, vin, vout, stack, s);
@@ -1172,6 +1249,16 @@ int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cuda
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
     if (W->box_cfg < 0) return RG_ERR_UNSUPPORTED;
     return launch_box_config(W, W->box_cfg, vin, vout, stack, s);
+}
+
+// The exact (float64) TMA apply: 4 slices per stage, 2 stages (FP64 issue,
+// not the staging, bounds it).
+int apply_box_exact(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s) {
+    if (W->box_state != 1) return RG_ERR_UNSUPPORTED;
+    const int bs = (int)std::min<int64_t>(4, stack);
+    CUtensorMap map;
+    if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
+    return launch_patch<4, 2, 0, true>(W, map, bs, vin, vout, stack, s);
 }
 
 // Whether the row kernel can take this call (the caller holds the lock and

@@ -606,6 +606,10 @@ def test_fast_apply_paths(rg, case, stack):
         # fewer slices than the tuned stage size (the warp-staged kernel takes over)
         one = dw.apply(d_vals[:1].contiguous(), accumulate="fast").cpu().numpy()
         assert_same(one, got[:1])
+    # the exact apply of the float32 stack: the upstream float64 result bit for bit
+    exact = dw.apply(d_vals, accumulate="exact").cpu().numpy()
+    assert exact.dtype == np.float64
+    assert_same(exact, oracle.apply(ii, oo, vv, vals, n_out))
     from regridding_gb300 import _lib
 
     _lib.call("rg_weights_check", dw.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))

@@ -36,6 +36,7 @@ import collections
 import ctypes
 import threading
 import time
+import weakref
 from concurrent.futures import Future, ThreadPoolExecutor
 from dataclasses import dataclass
 
@@ -63,9 +64,16 @@ def _hash_array(a: np.ndarray) -> tuple:
     return (a.dtype.str, a.shape, h1.value, h2.value)
 
 
+def _forget(memo: tuple) -> None:
+    with _key_memo_lock:
+        _key_memo.pop(memo, None)
+
+
 def grid_key(grid_input, grid_output) -> tuple:
     """Cache key of a grid pair: dtype, shape and two seeded 64-bit hashes of
-    every coordinate array.  Read-only arrays are hashed once per object."""
+    every coordinate array.  Read-only arrays are hashed once per object (the
+    memo holds a weak reference and is checked against the very object, so a
+    new array that reuses a freed one's address is hashed afresh)."""
     parts = []
     for a in (*grid_input, *grid_output):
         a = np.asarray(a)
@@ -73,13 +81,19 @@ def grid_key(grid_input, grid_output) -> tuple:
             memo = (id(a), a.__array_interface__["data"][0], a.shape)
             with _key_memo_lock:
                 hit = _key_memo.get(memo)
-            if hit is None:
-                hit = _hash_array(a)
-                with _key_memo_lock:
-                    if len(_key_memo) > 4096:
-                        _key_memo.clear()
-                    _key_memo[memo] = hit
-            parts.append(hit)
+            if hit is not None and hit[0]() is a:
+                parts.append(hit[1])
+                continue
+            h = _hash_array(a)
+            try:
+                ref = weakref.ref(a)
+            except TypeError:  # not weak-referenceable: no memo
+                parts.append(h)
+                continue
+            with _key_memo_lock:
+                _key_memo[memo] = (ref, h)
+            weakref.finalize(a, _forget, memo)
+            parts.append(h)
         else:
             parts.append(_hash_array(a))
     return tuple(parts)

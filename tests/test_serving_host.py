@@ -249,3 +249,24 @@ def test_cobuilds_share_one_batched_build():
         st = srv.stats()
     assert ["k1", "k2", "k3", "k4"] in be.build_calls  # one batched build for the four waiting grids
     assert st["builds"] == 4  # k0, k1, k2, k4
+
+
+def test_grid_key_memo_follows_the_object():
+    """A read-only array is hashed once; a new array that reuses a freed
+    one's memory and shape with other contents gets its own key."""
+    import gc
+
+    from regridding_gb300.serving import grid_key
+
+    def ro(v):
+        a = np.full((5, 5), v)
+        a.setflags(write=False)
+        return a
+
+    keys = set()
+    for v in range(20):
+        a, b = ro(v), ro(0.0)
+        keys.add(grid_key((a, b), (b, b)))
+        del a
+        gc.collect()
+    assert len(keys) == 20

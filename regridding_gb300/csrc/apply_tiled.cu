@@ -18,6 +18,7 @@
 
 #include <algorithm>
 #include <climits>
+#include <map>
 #include <cstdio>
 #include <cstdlib>
 
@@ -1193,14 +1194,36 @@ int forced_box_config() {
 }
 
 // Autotuner: on the first TMA apply of a handle, time every configuration
-// on the real call (each run writes the same result) and keep the fastest.
-// The caller holds the handle's lock; synchronises the stream.
+// on the real call (each run writes the same result) and keep the fastest;
+// later handles of the same kind (box height, stack size class) reuse the
+// choice without timing.  The caller holds the handle's lock; synchronises
+// the stream.
+// Tuned configurations shared by handles of the same kind: box height and
+// stack size class (1, 2-3, 4-7, ..., 64+) -> configuration.
+std::mutex g_tuned_mutex;
+std::map<std::pair<int, int>, int> g_tuned;
+
+int stack_class(int64_t stack) {
+    int c = 0;
+    while (c < 6 && ((int64_t)2 << c) <= stack) c++;
+    return c;
+}
+
 int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
     if (W->box_cfg >= 0) return RG_OK;
     const int forced = forced_box_config();
     if (forced >= 0) {
         W->box_cfg = forced;
         return RG_OK;
+    }
+    const std::pair<int, int> kind(W->box_rows, stack_class(stack));
+    {
+        std::lock_guard<std::mutex> lock(g_tuned_mutex);
+        auto it = g_tuned.find(kind);
+        if (it != g_tuned.end()) {
+            W->box_cfg = it->second;
+            return RG_OK;
+        }
     }
     cudaEvent_t e0 = nullptr, e1 = nullptr;
     RG_CUDA(cudaEventCreate(&e0));
@@ -1240,6 +1263,10 @@ int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cuda
     cudaEventDestroy(e1);
     if (st != RG_OK) return st;
     W->box_cfg = best >= 0 ? best : -2;
+    if (best >= 0) {
+        std::lock_guard<std::mutex> lock(g_tuned_mutex);
+        g_tuned[kind] = best;
+    }
     return RG_OK;
 }
 

@@ -35,6 +35,7 @@
 #include <vector>
 
 #include "common.cuh"
+#include "seed.cuh"
 
 namespace rg {
 namespace {
@@ -745,16 +746,6 @@ __device__ __forceinline__ int family_of_chunk(const ChunkPlan& C, int64_t g) {
     return f;
 }
 
-__device__ __forceinline__ double bilinear_fast(const double* a, int64_t sx, int64_t sy, double x, double y) {
-    int64_t x0 = (int64_t)floor(x), y0 = (int64_t)floor(y);
-    x0 = x0 < 0 ? 0 : (x0 > sx - 2 ? sx - 2 : x0);
-    y0 = y0 < 0 ? 0 : (y0 > sy - 2 ? sy - 2 : y0);
-    double dx = x - x0, dy = y - y0;
-    double a00 = __ldg(a + x0 * sy + y0), a01 = __ldg(a + x0 * sy + y0 + 1);
-    double a10 = __ldg(a + (x0 + 1) * sy + y0), a11 = __ldg(a + (x0 + 1) * sy + y0 + 1);
-    return a00 * (1 - dx) * (1 - dy) + a01 * (1 - dx) * dy + a10 * dx * (1 - dy) + a11 * dx * dy;
-}
-
 // A guess of the walk state at a sweep vertex: the static cell containing
 // it (Newton seed on the bilinear index map, then a walk across the edge the
 // point lies beyond), or "outside".  Wrong guesses are fixed by the repair.
@@ -763,25 +754,8 @@ __device__ WalkState guess_state(const Static& S, double px, double py, int64_t 
     if (!((S.blx <= px && px <= S.bux) && (S.bly <= py && py <= S.buy))) return w;
     const Grid& g = S.g;
     const int64_t ncx = S.ncx, ncy = S.ncy;
-    double fi = 0.5 * (double)ncx, fj = 0.5 * (double)ncy;
-    for (int it = 0; it < 10; it++) {
-        double xv = bilinear_fast(g.x, g.nx, g.ny, fi, fj), yv = bilinear_fast(g.y, g.nx, g.ny, fi, fj);
-        const double h = 1e-3;
-        double xi = (bilinear_fast(g.x, g.nx, g.ny, fi + h, fj) - xv) / h;
-        double xj = (bilinear_fast(g.x, g.nx, g.ny, fi, fj + h) - xv) / h;
-        double yi = (bilinear_fast(g.y, g.nx, g.ny, fi + h, fj) - yv) / h;
-        double yj = (bilinear_fast(g.y, g.nx, g.ny, fi, fj + h) - yv) / h;
-        double det = xi * yj - xj * yi;
-        if (!(det != 0) || !isfinite(det)) break;
-        double ex = xv - px, ey = yv - py;
-        double di = (yj * ex - xj * ey) / det, dj = (-yi * ex + xi * ey) / det;
-        fi = fmin(fmax(fi - di, 0.0), (double)ncx - 1e-9);
-        fj = fmin(fmax(fj - dj, 0.0), (double)ncy - 1e-9);
-        if (fabs(di) < 1e-3 && fabs(dj) < 1e-3) break;
-    }
-    int64_t ci = (int64_t)floor(fi), cj = (int64_t)floor(fj);
-    ci = ci < 0 ? 0 : (ci >= ncx ? ncx - 1 : ci);
-    cj = cj < 0 ? 0 : (cj >= ncy ? ncy - 1 : cj);
+    int64_t ci, cj;
+    seed_cell(g.x, g.y, g.nx, g.ny, px, py, &ci, &cj);
     for (int step = 0; step < 64; step++) {
         if (cell_contains(g, ci, cj, px, py)) {
             w.stx = ci;

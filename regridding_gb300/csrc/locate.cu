@@ -17,6 +17,7 @@
 #include <mutex>
 
 #include "common.cuh"
+#include "seed.cuh"
 
 namespace rg {
 namespace {
@@ -85,16 +86,6 @@ __device__ void lowest_local(const G2& g, double px, double py, int64_t i0, int6
     *oj = j0;
 }
 
-__device__ __forceinline__ double bilin(const double* a, int64_t sx, int64_t sy, double x, double y) {
-    int64_t x0 = (int64_t)floor(x), y0 = (int64_t)floor(y);
-    x0 = x0 < 0 ? 0 : (x0 > sx - 2 ? sx - 2 : x0);
-    y0 = y0 < 0 ? 0 : (y0 > sy - 2 ? sy - 2 : y0);
-    double dx = x - x0, dy = y - y0;
-    double a00 = __ldg(a + x0 * sy + y0), a01 = __ldg(a + x0 * sy + y0 + 1);
-    double a10 = __ldg(a + (x0 + 1) * sy + y0), a11 = __ldg(a + (x0 + 1) * sy + y0 + 1);
-    return a00 * (1 - dx) * (1 - dy) + a01 * (1 - dx) * dy + a10 * dx * (1 - dy) + a11 * dx * dy;
-}
-
 __global__ void __launch_bounds__(128)
     locate_walk_kernel(G2 g, const double* __restrict__ px, const double* __restrict__ py, int64_t n,
                        int64_t* __restrict__ oi, int64_t* __restrict__ oj, int64_t* __restrict__ fails,
@@ -103,28 +94,9 @@ __global__ void __launch_bounds__(128)
     if (k >= n) return;
     const int64_t ncx = g.nx - 1, ncy = g.ny - 1;
     const double p_x = px[k], p_y = py[k];
-    // Newton seed on the bilinear index map (forward differences)
-    double fi = 0.5 * (double)ncx, fj = 0.5 * (double)ncy;
-    for (int it = 0; it < 12; it++) {
-        double xv = bilin(g.x, g.nx, g.ny, fi, fj), yv = bilin(g.y, g.nx, g.ny, fi, fj);
-        double ex = xv - p_x, ey = yv - p_y;
-        const double h = 1e-3;
-        double xi = (bilin(g.x, g.nx, g.ny, fi + h, fj) - xv) / h;
-        double xj = (bilin(g.x, g.nx, g.ny, fi, fj + h) - xv) / h;
-        double yi = (bilin(g.y, g.nx, g.ny, fi + h, fj) - yv) / h;
-        double yj = (bilin(g.y, g.nx, g.ny, fi, fj + h) - yv) / h;
-        double det = xi * yj - xj * yi;
-        if (!(det != 0) || !isfinite(det)) break;
-        double di = (yj * ex - xj * ey) / det, dj = (-yi * ex + xi * ey) / det;
-        fi -= di;
-        fj -= dj;
-        fi = fmin(fmax(fi, 0.0), (double)ncx - 1e-9);
-        fj = fmin(fmax(fj, 0.0), (double)ncy - 1e-9);
-        if (fabs(di) < 1e-3 && fabs(dj) < 1e-3) break;
-    }
-    int64_t ci = (int64_t)floor(fi), cj = (int64_t)floor(fj);
-    ci = ci < 0 ? 0 : (ci >= ncx ? ncx - 1 : ci);
-    cj = cj < 0 ? 0 : (cj >= ncy ? ncy - 1 : cj);
+    // starting guess: Newton on the bilinear index map (float32)
+    int64_t ci, cj;
+    seed_cell(g.x, g.y, g.nx, g.ny, p_x, p_y, &ci, &cj);
     const int cap = 64 + 2 * (int)sqrt((double)(ncx + ncy));
     for (int step = 0; step < cap; step++) {
         if (contains(g, ci, cj, p_x, p_y)) {

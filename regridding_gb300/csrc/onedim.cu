@@ -226,7 +226,13 @@ __global__ void conservative_1d_kernel(const double* __restrict__ xin, int64_t i
 // Per-row keys for ordering conservative 1D entries by (input, output):
 // negative (reversed-grid) indices are shifted by the row length, which keeps
 // their order because a row's indices all have the same sign.
-__global__ void conservative_1d_keys(const int64_t* __restrict__ ind_in,
+// Unused slots of a row (j >= count) are marked with PAD_INDEX and spread
+// over the row's own buckets with keys that sort after every real entry, so
+// no bucket grows long (the within-bucket ranking of long buckets is the
+// expensive part of the sort); the merge skips them.
+constexpr int64_t PAD_INDEX = INT64_MIN;
+
+__global__ void conservative_1d_keys(int64_t* __restrict__ ind_in,
                                      const int64_t* __restrict__ ind_out,
                                      const int64_t* __restrict__ count, int64_t nd, int64_t cap,
                                      int64_t m, int64_t n, int32_t* __restrict__ bucket,
@@ -242,8 +248,9 @@ __global__ void conservative_1d_keys(const int64_t* __restrict__ ind_in,
             bucket[k] = (int32_t)(d * (m - 1) + i);
             skey[k] = (o << 32) | (int64_t)j;
         } else {
-            bucket[k] = (int32_t)(nd * (m - 1));  // parking bucket past the last row
-            skey[k] = j;
+            ind_in[k] = PAD_INDEX;
+            bucket[k] = (int32_t)(d * (m - 1) + j % (m - 1));
+            skey[k] = ((int64_t)INT32_MAX << 32) | (int64_t)j;
         }
     }
 }
@@ -265,6 +272,10 @@ __global__ void conservative_1d_merge(const uint32_t* __restrict__ perm, const i
     while (g < t) {
         uint32_t e = perm[g];
         int64_t ii = in_raw[e], oo = out_raw[e];
+        if (ii == PAD_INDEX) {  // unused slot (sorted last in its bucket)
+            g++;
+            continue;
+        }
         double acc = val_raw[e];
         // group of equal pairs: first + (sequential from -0.0 over the rest,
         // exact for the < 8 extra terms a 1D overlap can produce)
@@ -404,7 +415,7 @@ int conservative_1d(const double* xin, int64_t in_stride, int64_t m, const doubl
                     cudaStream_t s) {
     RG_CHECK(m >= 2 && n >= 2, RG_ERR_ARG, "conservative 1D: grids need at least 2 vertices");
     if (nd <= 0) return RG_OK;
-    RG_CHECK(nd * (m - 1) + 1 < INT32_MAX && nd * cap < UINT32_MAX, RG_ERR_UNSUPPORTED,
+    RG_CHECK(nd * (m - 1) < INT32_MAX && nd * cap < UINT32_MAX, RG_ERR_UNSUPPORTED,
              "conservative 1D: batch too large");
     int64_t total = nd * cap;
     int64_t *r_in = nullptr, *r_out = nullptr, *skey = nullptr, *bptr = nullptr;
@@ -427,7 +438,7 @@ int conservative_1d(const double* xin, int64_t in_stride, int64_t m, const doubl
         unsigned g = grid_for(total, 256);
         if (g > 65536) g = 65536;
         conservative_1d_keys<<<g, 256, 0, s>>>(r_in, r_out, count, nd, cap, m, n, bucket, skey);
-        int64_t nb = nd * (m - 1) + 1;
+        int64_t nb = nd * (m - 1);
         if ((st = dalloc(&bptr, (size_t)nb + 1, s))) break;
         if ((st = dalloc(&perm, (size_t)total, s))) break;
         if ((st = bucket_sort(bucket, skey, total, nb, bptr, perm, nullptr, s))) break;

@@ -327,6 +327,38 @@ def run_serving(args, torch):
     return out
 
 
+def run_conservative_1d(args, torch):
+    """Per-spectrum 1D conservative weights at scale (the next item after the
+    2D path): 10^5 spectra, each with its own sorted input grid of 1025 edges
+    and output grid of 769 edges, through the public weights() (saved layout:
+    one element per spectrum); the CPU oracle builds a 10^3-spectrum sample."""
+    import oracle
+    import regridding_gb300 as rg
+
+    rng = np.random.default_rng(14)
+    nd, m, n = 100_000, 1025, 769
+    x_in = np.sort(rng.uniform(0, 1, (nd, m)), axis=1)
+    x_out = np.sort(rng.uniform(0, 1, (nd, n)), axis=1)
+    ts = []
+    for _ in range(2):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        w, _, _ = rg.weights(x_in, x_out, axis_input=1, axis_output=1, method="conservative")
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    same = all(all(np.array_equal(a, b) for a, b in zip(w[k], oracle.conservative_1d(x_in[k], x_out[k])))
+               for k in (0, 1, nd // 2, nd - 1))
+    t0 = time.perf_counter()
+    for k in range(1000):
+        oracle.conservative_1d(x_in[k], x_out[k])
+    t_cpu = time.perf_counter() - t0
+    return {"workload": "1D conservative, 10^5 spectra, 1025 -> 769 edges each, per-spectrum grids",
+            "weights_ms": round(min(ts) * 1e3, 1), "spectra_per_s": round(nd / min(ts), 0),
+            "bit_identical_to_oracle_sample": same,
+            "cpu_baseline": {"spectra_per_s": round(1000 / t_cpu, 0), "cores": 1, "kind": "port",
+                             "sample": "10^3 spectra, one thread"}}
+
+
 def run_batched(args, torch):
     """256 uneven grid pairs (sides log-uniform in [64, 1024] cells, random
     rotation and sinusoidal distortion of amplitude uniform(0, 0.03), output
@@ -660,6 +692,7 @@ def run_ours(args, world, rank, local):
         line["serving"] = run_serving(args, torch)
     if rank == 0 and not args.no_extra:
         line["multilinear_1d"] = run_multilinear_1d(args, torch)
+        line["conservative_1d"] = run_conservative_1d(args, torch)
         line["batched"] = run_batched(args, torch)
         line["differentiable"] = run_differentiable(args, torch)
     if rank == 0:

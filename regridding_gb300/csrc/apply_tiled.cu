@@ -1,19 +1,23 @@
-// Warp-tiled apply: the float32 fast path of rg_apply.
+// Staged applies: the float32 fast path of rg_apply and the exact float64
+// apply of float32 stacks.
 //
 // The plain kernel (apply.cu) gathers every input value straight from global
 // memory; on a rotated grid the 32 gathers of a warp touch ~10 sectors spread
 // over several input rows, so the L1 data pipe and instruction issue, not
-// HBM, bound it.  Here every warp owns a compact 4 x 8 patch of output cells
-// (a "warp tile", one cell per lane).  Once per weights matrix, each warp
-// tile gets the sorted list of distinct 32-byte sectors (8 consecutive input
-// cells) its rows read, and every stored entry gets the slot of its cell in
-// that list.  The apply runs warp by warp with no block-wide
-// synchronisation: for every group of 4 stack slices each lane loads one
-// sector of the 4 slices with 128-bit loads (every fetched sector is one the
-// tile needs), transposes it in registers and stores it to the warp's
-// shared-memory stage interleaved by slice; each entry of a lane's row is
-// then one 128-bit shared load that serves all 4 slices.  A second, scalar variant handles
-// inputs whose slices are not 16-byte aligned.
+// HBM, bound it.  The kernels here stage input in shared memory first:
+//
+// * apply_patch_tma (input grid shape known): a block of 8 warps owns a
+//   16 x 16 patch of output cells; tensor-map copies (TMA) bring the patch's
+//   input box for a few slices at a time into a ring of stages behind
+//   full/empty mbarriers; lanes gather from shared memory in a bank-aware
+//   order.  Its EXACT form reproduces the upstream float64 sums bit for bit.
+// * apply_rows (short input axis, long stacks): whole slices by 1D bulk
+//   copies, entries held in registers.
+// * apply_warp_vec / apply_warp_scalar (no shapes): every warp owns a 4 x 8
+//   patch, loads the sorted list of input sectors its rows read with 128-bit
+//   loads and restages it interleaved by slice, so that each entry is one
+//   128-bit shared load serving 4 slices (the scalar form for unaligned
+//   slices).
 #include <cuda.h>  // CUtensorMap and its enums; the encoder comes from the runtime's driver entry point
 
 #include <algorithm>

@@ -274,8 +274,12 @@ def run_serving(args, torch):
             p50, p99 = percentiles(lat)
             new = [f.request.t_done - f.request.t_arrival for f, r in zip(futs, reqs) if r["cached"] < 0]
             old = [f.request.t_done - f.request.t_arrival for f, r in zip(futs, reqs) if r["cached"] >= 0]
+            nq = [f.request for f, r in zip(futs, reqs) if r["cached"] < 0]
             out[mode] = {"req_per_s": round(n_req / (t_end - t0), 1), "p50_ms": p50, "p99_ms": p99,
                          "p50_p99_ms_resident_grid": percentiles(old), "p50_p99_ms_new_grid": percentiles(new),
+                         "new_grid_p50_p99_ms": {"wait": percentiles([q.t_start - q.t_arrival for q in nq]),
+                                                 "build": percentiles([q.t_built - q.t_start for q in nq]),
+                                                 "copy_apply_copy": percentiles([q.t_done - q.t_built for q in nq])},
                          "mean_batch": round(float(np.mean([f.request.batch for f in futs])), 2),
                          "server": {k: v for k, v in srv.stats().items() if k != "budget"}}
     torch.cuda.synchronize()

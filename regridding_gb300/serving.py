@@ -210,6 +210,8 @@ class _Request:
     future: Future
     t_arrival: float
     result: object = None
+    t_start: float = 0.0  # its job started on a slot
+    t_built: float = 0.0  # its weights were ready (build jobs)
     t_done: float = 0.0
     batch: int = 0
 
@@ -249,8 +251,34 @@ class GpuBackend:
                                                                perturb=True, seed=self.seed)
         return gi, go
 
+    class Slot:
+        """A slot's compute stream and the stream its input copies use."""
+
+        def __init__(self, torch):
+            self.stream = torch.cuda.Stream()
+            self.copy = torch.cuda.Stream()
+
     def make_slot(self, index: int):
-        return self.torch.cuda.Stream()
+        return GpuBackend.Slot(self.torch)
+
+    def stage(self, slot, requests: list):
+        """Start copying the requests' stacks to one device buffer on the
+        slot's copy stream (so that they travel while the weights build);
+        returns the buffer and the event that marks the copies' end."""
+        t = self.torch
+        vdt = requests[0].values.dtype
+        if not all(r.values.dtype == vdt for r in requests):
+            vdt = t.float64
+        n_in = requests[0].n_in
+        with t.cuda.stream(slot.copy):
+            vin = t.empty((sum(r.stack for r in requests), n_in), dtype=vdt, device="cuda")
+            off = 0
+            for r in requests:
+                vin[off:off + r.stack].copy_(r.values, non_blocking=True)
+                off += r.stack
+            done = t.cuda.Event()
+            done.record(slot.copy)
+        return vin, done
 
     def prepare(self, values, out, n_in: int, n_out: int):
         """Host tensors for a request: values viewed as (stack, n_in); out
@@ -278,7 +306,7 @@ class GpuBackend:
 
     def build(self, slot, req: _Request):
         gi, go = self.grids(req.grid_input, req.grid_output)
-        with self.torch.cuda.stream(slot):
+        with self.torch.cuda.stream(slot.stream):
             dw = _device.build_conservative_2d(gi, go)
             nbytes = ctypes.c_int64()
             _lib.call("rg_weights_device_bytes", dw.handle, ctypes.byref(nbytes))
@@ -289,7 +317,7 @@ class GpuBackend:
         """Weights of several grid pairs in one batched build: per request
         (weights, device bytes) or the exception of its failed build."""
         pairs = [self.grids(r.grid_input, r.grid_output) for r in reqs]
-        with self.torch.cuda.stream(slot):
+        with self.torch.cuda.stream(slot.stream):
             built = _device.build_conservative_2d_batch(pairs)
         out = []
         for dw in built:
@@ -301,19 +329,23 @@ class GpuBackend:
             out.append((dw, nbytes.value + dw.nnz * 6 + (dw.n_out // 32 + 1) * 16))
         return out
 
-    def run(self, slot, weights, requests: list) -> None:
+    def run(self, slot, weights, requests: list, staged=None) -> None:
         t = self.torch
-        with t.cuda.stream(slot):
-            total = sum(r.stack for r in requests)
-            vdt = requests[0].values.dtype
-            same = all(r.values.dtype == vdt for r in requests)
-            if not same:
-                vdt = t.float64
-            vin = t.empty((total, weights.n_in), dtype=vdt, device="cuda")
-            off = 0
-            for r in requests:
-                vin[off:off + r.stack].copy_(r.values, non_blocking=True)
-                off += r.stack
+        with t.cuda.stream(slot.stream):
+            if staged is not None:
+                vin, done = staged
+                slot.stream.wait_event(done)
+                vin.record_stream(slot.stream)  # used on this stream too (allocator bookkeeping)
+            else:
+                vdt = requests[0].values.dtype
+                if not all(r.values.dtype == vdt for r in requests):
+                    vdt = t.float64
+                vin = t.empty((sum(r.stack for r in requests), weights.n_in), dtype=vdt, device="cuda")
+                off = 0
+                for r in requests:
+                    vin[off:off + r.stack].copy_(r.values, non_blocking=True)
+                    off += r.stack
+            total = vin.shape[0]
             odt = requests[0].out.dtype
             out = weights.apply(vin, out=t.empty((total, weights.n_out), dtype=odt, device="cuda"),
                                 accumulate=self.accumulate)
@@ -321,7 +353,7 @@ class GpuBackend:
             for r in requests:
                 r.out.copy_(out[off:off + r.stack], non_blocking=True)
                 off += r.stack
-            slot.synchronize()
+            slot.stream.synchronize()
 
     def free(self, weights) -> None:
         weights.free()
@@ -595,7 +627,12 @@ class RegridServer:
         err = None
         built = False
         cobuild = job.cobuild or []
+        staged = None
+        t_built = job.t_start
         try:
+            if job.build and hasattr(self.backend, "stage"):
+                # the stacks travel to the device while the weights build
+                staged = self.backend.stage(stream, job.requests)
             if job.build:
                 if cobuild:
                     results = self.backend.build_many(stream, [job.requests[0]] + cobuild)
@@ -626,7 +663,11 @@ class RegridServer:
                     raise results[0]
                 job.weights = results[0][0]
                 built = True
-            self.backend.run(stream, job.weights, job.requests)
+            t_built = time.perf_counter()
+            if staged is not None:
+                self.backend.run(stream, job.weights, job.requests, staged)
+            else:
+                self.backend.run(stream, job.weights, job.requests)
         except Exception as e:  # noqa: BLE001 - reported through the futures
             err = e
         t_done = time.perf_counter()
@@ -643,6 +684,8 @@ class RegridServer:
             self.n_done += len(job.requests)
             self._cv.notify_all()
         for r in job.requests:
+            r.t_start = job.t_start
+            r.t_built = t_built if err is None or built else job.t_start
             r.t_done = t_done
             r.batch = len(job.requests)
             if err is not None:
@@ -670,11 +713,12 @@ def regrid_plain(grid_input, grid_output, values, accumulate: str = "fast", out=
     n_in = (gi[0].shape[0] - 1) * (gi[0].shape[1] - 1)
     n_out = (go[0].shape[0] - 1) * (go[0].shape[1] - 1)
     v, o = backend.prepare(values, out, n_in, n_out)
-    stream = t.cuda.current_stream()
+    slot = GpuBackend.Slot.__new__(GpuBackend.Slot)
+    slot.stream = slot.copy = t.cuda.current_stream()  # one call at a time: everything in order
     dw = _device.build_conservative_2d(*backend.grids(gi, go))
     try:
         req = _Request(gi, go, v, o, int(v.shape[0]), n_in, n_out, (), Future(), 0.0)
-        backend.run(stream, dw, [req])
+        backend.run(slot, dw, [req])
     finally:
         dw.free()
     return o

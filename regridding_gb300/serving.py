@@ -588,6 +588,8 @@ class RegridServer:
             for r in group:
                 self._pending.remove(r)
             weights = self.cache.acquire(head.key) if cached else None
+            if not cached:
+                self.cache.misses += 1
             job = _Job(head.key, group, not cached, footprint, weights)
             if not cached and self.max_cobuild > 0 and head.n_in <= self.cobuild_max_cells:
                 # other small grids waiting for weights go into the same batched build

@@ -68,3 +68,49 @@ def test_product_refuses_without_gpu():
 
     with pytest.raises(rg.RegridError):
         rg.find_indices((np.linspace(0, 1, 5),), (np.linspace(0, 1, 3),))
+
+
+def test_batch_and_option_arguments_need_no_gpu():
+    L = _lib.load()
+    for name, args in _lib.SIGNATURES.items():
+        getattr(L, name).argtypes = args
+    out = (ctypes.c_void_p * 1)()
+    status = (ctypes.c_int * 1)()
+    assert L.rg_build_conservative_2d_batch(0, None, None, None, None, None, None, None, None, None, None, out,
+                                            status) == _lib.RG_ERR_ARG
+    assert L.rg_build_conservative_2d_batch(1, None, None, None, None, None, None, None, None, None, None, out,
+                                            status) == _lib.RG_ERR_ARG
+    assert L.rg_set_sweep_chunk(-1) == _lib.RG_ERR_ARG
+    assert L.rg_set_sweep_chunk(32) == _lib.RG_OK
+    assert L.rg_weights_check(None, None) == _lib.RG_ERR_ARG
+    assert L.rg_weights_set_input_shape(None, 1, 1) == _lib.RG_ERR_ARG
+    assert L.rg_weights_device_bytes(None, None) == _lib.RG_ERR_ARG
+    assert L.rg_conservative_2d_grad_output(None, None, None, 2, 2, None, None, 2, 2, None, None, None, 0, 1,
+                                            None, None, None, None) == _lib.RG_ERR_ARG
+
+
+def test_hash64_is_a_host_function():
+    """rg_hash64 runs on the host (no GPU): deterministic, seed- and
+    content-sensitive, and the same on both sides of the 4 MiB segmented
+    path's threshold whatever thread count hashes the segments."""
+    import numpy as np
+
+    L = _lib.load()
+
+    def h(a, seed=7):
+        out = ctypes.c_uint64()
+        assert L.rg_hash64(ctypes.c_void_p(a.ctypes.data), a.nbytes, seed, ctypes.byref(out)) == _lib.RG_OK
+        return out.value
+
+    rng = np.random.default_rng(0)
+    for n in (0, 1, 31, 32, 33, 1000, (4 << 20) // 8, (4 << 20) // 8 + 1, 3_000_000):
+        a = rng.random(n)
+        assert h(a) == h(a.copy())
+        if n:
+            b = a.copy()
+            b[n // 2] = np.nextafter(b[n // 2], 2.0)
+            assert h(b) != h(a)
+            assert h(a, 8) != h(a, 7)
+    out = ctypes.c_uint64()
+    assert L.rg_hash64(None, 8, 0, ctypes.byref(out)) == _lib.RG_ERR_ARG
+    assert L.rg_hash64(None, 0, 0, ctypes.byref(out)) == _lib.RG_OK

@@ -289,6 +289,18 @@ int rg_conservative_2d_grad_output(rg_weights w, const double* d_xi, const doubl
                                    const void* d_grad_out, int dtype, int64_t stack, double* d_grad_xo,
                                    double* d_grad_yo, double* d_w_check, rg_stream_t stream);
 
+/* Linear (ny == 0) or bilinear interpolation of n_orth arrays at m index
+ * points each: ndarray_linear_interpolation, regridding/_interp_ndarray.py
+ * :11-268.  Array e has nx (x ny) float64 samples at d_a + e * a_stride and
+ * its points' fractional indices at d_x (and d_y) + e * i_stride (a stride of
+ * 0 shares one array or one set of points); d_out receives n_orth x m
+ * float64 values.  Cells are floor(index) clamped to the first/last cell
+ * (linear extrapolation outside), with the upstream operation order.
+ * nx >= 2 and ny == 0 or ny >= 2 (RG_ERR_ARG otherwise). */
+int rg_interp_linear(const double* d_a, int64_t a_stride, int64_t nx, int64_t ny, const double* d_x,
+                     const double* d_y, int64_t i_stride, int64_t m, int64_t n_orth, double* d_out,
+                     rg_stream_t stream);
+
 /* Device bytes currently held by a handle: the CSR plus whatever state
  * applies have made on first use (float32 weights, tile lists, transposed
  * CSR).  Used by caches that account weights against an HBM budget.  No

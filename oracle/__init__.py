@@ -269,3 +269,56 @@ def conservative_1d(x_input, x_output, weights_input=None):
     if n < 0:
         raise RuntimeError("oracle conservative_1d capacity exceeded")
     return ind_in[:n].copy(), ind_out[:n].copy(), val[:n].copy()
+
+
+def ndarray_linear_interpolation(a, indices, axis=None, axis_indices=None):
+    """``ndarray_linear_interpolation`` (regridding/_interp_ndarray.py:11-223):
+    the axis bookkeeping of :66-163 and the point formulas of
+    ``_linear_interpolation`` (:192-217) and ``_bilinear_interpolation``
+    (:220-268), vectorised with numpy in the same operation order (one
+    rounding per operation, as the pure-Python evaluation does)."""
+    a = np.asarray(a)
+    ndim_a = a.ndim
+    b = np.broadcast(*indices)
+    shape_i, ndim_i = b.shape, b.ndim
+    if axis is None:
+        axis = tuple(range(ndim_a))
+    axis = np.lib.array_utils.normalize_axis_tuple(axis, ndim=ndim_a)
+    axis = tuple(int(v) for v in ~(~np.array(axis) % ndim_a))
+    if axis_indices is None:
+        axis_indices = tuple(range(ndim_i))
+    axis_indices = np.lib.array_utils.normalize_axis_tuple(axis_indices, ndim=ndim_i)
+    axis_indices = tuple(int(v) for v in ~(~np.array(axis_indices) % ndim_i))
+    if len(indices) != len(axis):
+        raise ValueError("number of indices must match the number of axes")
+    orth_a = tuple(ax for ax in range(-ndim_a, 0) if ax not in axis)
+    orth_i = tuple(ax for ax in range(-ndim_i, 0) if ax not in axis_indices)
+    shape_orth = np.broadcast_shapes(tuple(a.shape[ax] for ax in orth_a), tuple(shape_i[ax] for ax in orth_i))
+    nba, nbi = len(shape_orth) + len(axis), len(shape_orth) + len(axis_indices)
+    shape_ba = tuple(a.shape[ax] if ax in axis else shape_orth[orth_a.index(ax)] for ax in range(-nba, 0))
+    shape_bi = tuple(shape_i[ax] if ax in axis_indices else shape_orth[orth_i.index(ax)] for ax in range(-nbi, 0))
+    a = np.broadcast_to(a, shape_ba)
+    idx = tuple(np.broadcast_to(i, shape_bi) for i in indices)
+    result = np.empty(shape_bi)
+    for index in np.ndindex(*shape_orth):
+        ia = tuple(slice(None) if ax in axis else index[orth_a.index(ax)] for ax in range(-nba, 0))
+        ii = tuple(slice(None) if ax in axis_indices else index[orth_i.index(ax)] for ax in range(-nbi, 0))
+        s = a[ia]
+        if len(axis) == 1:
+            x = idx[0][ii].reshape(-1).astype(float)
+            x0 = np.clip(np.floor(x).astype(np.int64), 0, s.shape[0] - 2)
+            dx = x - x0
+            r = s[x0] * (1 - dx) + s[x0 + 1] * dx
+        elif len(axis) == 2:
+            x = idx[0][ii].reshape(-1).astype(float)
+            y = idx[1][ii].reshape(-1).astype(float)
+            x0 = np.clip(np.floor(x).astype(np.int64), 0, s.shape[0] - 2)
+            y0 = np.clip(np.floor(y).astype(np.int64), 0, s.shape[1] - 2)
+            dx, dy = x - x0, y - y0
+            w00, w01 = (1 - dx) * (1 - dy), (1 - dx) * dy
+            w10, w11 = dx * (1 - dy), dx * dy
+            r = (s[x0, y0] * w00) + (s[x0, y0 + 1] * w01) + (s[x0 + 1, y0] * w10) + (s[x0 + 1, y0 + 1] * w11)
+        else:
+            raise NotImplementedError
+        result[ii] = r.reshape(idx[0][ii].shape)
+    return result

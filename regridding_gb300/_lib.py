@@ -35,6 +35,7 @@ SIGNATURES = {
     "rg_last_error": [ctypes.c_char_p, ctypes.c_size_t],
     "rg_build_conservative_2d": [_P, _P, _I, _I, _P, _P, _I, _I, _P, _P, ctypes.POINTER(_P)],
     "rg_set_sweep_chunk": [_I],
+    "rg_interp_linear": [_P, _I, _I, _I, _P, _P, _I, _I, _I, _P, _P],
     "rg_build_conservative_2d_batch": [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "rg_weights_from_coo": [_P, _P, _P, _I, _I, _I, _P, ctypes.POINTER(_P)],
     "rg_weights_info": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)],

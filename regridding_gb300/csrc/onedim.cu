@@ -488,4 +488,73 @@ int transpose_conservative_scale(const int64_t* ii, const int64_t* oo, const dou
     return RG_OK;
 }
 
+namespace {
+
+// ndarray_linear_interpolation (regridding/_interp_ndarray.py:166-268): one
+// thread per output point; element e of the orthogonal batch reads its
+// samples at a + e * a_stride (stride 0: one array for all elements) and its
+// indices at x + e * i_stride (likewise).  The cell is floor(x) moved into
+// [0, n - 2] (linear extrapolation outside, :208-213), and the point formulas
+// keep the upstream operation order with one rounding per operation.  The
+// host guarantees n >= 2 on every interpolated axis, so all four reads stay
+// inside the array; floor() of a huge or NaN index converts with saturation
+// and is then clamped like any other.
+__device__ __forceinline__ int64_t interp_cell(double v, int64_t n) {
+    int64_t c = (int64_t)floor(v);
+    if (c < 0) c = 0;
+    else if (c > n - 2) c = n - 2;
+    return c;
+}
+
+__global__ void interp_kernel(const double* __restrict__ a, int64_t a_stride, int64_t nx, int64_t ny,
+                              const double* __restrict__ x, const double* __restrict__ y, int64_t i_stride,
+                              int64_t m, int64_t n_orth, double* __restrict__ out) {
+    const int64_t total = n_orth * m;
+    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
+         k += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t e = k / m, p = k - e * m;
+        const double* s = a + e * a_stride;
+        const double xv = x[e * i_stride + p];
+        const int64_t x0 = interp_cell(xv, nx);
+        const double dx = dsub(xv, (double)x0);
+        const int64_t i0 = x0, i1 = x0 + 1;
+        double r;
+        if (ny == 0) {
+            r = dadd(dmul(s[i0], dsub(1.0, dx)), dmul(s[i1], dx));
+        } else {
+            const double yv = y[e * i_stride + p];
+            const int64_t y0 = interp_cell(yv, ny);
+            const double dy = dsub(yv, (double)y0);
+            const int64_t j0 = y0, j1 = y0 + 1;
+            const double w00 = dmul(dsub(1.0, dx), dsub(1.0, dy));
+            const double w01 = dmul(dsub(1.0, dx), dy);
+            const double w10 = dmul(dx, dsub(1.0, dy));
+            const double w11 = dmul(dx, dy);
+            r = dadd(dadd(dadd(dmul(s[i0 * ny + j0], w00), dmul(s[i0 * ny + j1], w01)), dmul(s[i1 * ny + j0], w10)),
+                     dmul(s[i1 * ny + j1], w11));
+        }
+        out[k] = r;
+    }
+}
+
+}  // namespace
+
 }  // namespace rg
+
+extern "C" int rg_interp_linear(const double* d_a, int64_t a_stride, int64_t nx, int64_t ny, const double* d_x,
+                                const double* d_y, int64_t i_stride, int64_t m, int64_t n_orth, double* d_out,
+                                rg_stream_t stream) {
+    using namespace rg;
+    RG_CHECK(nx >= 2 && (ny == 0 || ny >= 2) && m >= 0 && n_orth >= 0 && a_stride >= 0 && i_stride >= 0, RG_ERR_ARG,
+             "rg_interp_linear: every interpolated axis needs at least 2 samples");
+    RG_CHECK(ny == 0 || d_y, RG_ERR_ARG, "rg_interp_linear: 2D interpolation needs y indices");
+    if (m == 0 || n_orth == 0) return RG_OK;
+    RG_CHECK(d_a && d_x && d_out, RG_ERR_ARG, "rg_interp_linear: NULL argument");
+    const int64_t total = n_orth * m;
+    const unsigned grid = grid_for(total, 256) > 16384 ? 16384 : grid_for(total, 256);
+    interp_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_a, a_stride, nx, ny, d_x, d_y, i_stride, m, n_orth,
+                                                          d_out);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+

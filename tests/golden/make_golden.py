@@ -3,7 +3,7 @@
 Run from the repository root (needs the upstream source tree, not available on
 GPU hosts):
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [known] [one_dim] [curvilinear] [interp]
 
 The upstream package is imported in its JIT-disabled pure-Python mode through
 ``reference_env`` (the mode its own CI exercises).  Each case below restates
@@ -478,20 +478,81 @@ def gen_curvilinear(store: Store):
                                                                weights_input=wi, method="conservative"))
 
 
-def main():
-    s = Store()
-    gen_conservative_2d(s)
-    gen_layout_and_seed(s)
-    gen_transposes(s)
-    gen_grids(s)
-    s.save("known_answers.npz")
-    s = Store()
-    gen_1d(s)
-    s.save("one_dim.npz")
-    s = Store()
-    gen_curvilinear(s)
-    s.save("curvilinear.npz")
+# ---------------------------------------------------------------------------
+# ndarray_linear_interpolation: regridding/_tests/test_interp_ndarray.py:11-93
+# (same array sizes and index families; seeded values) plus extrapolated
+# indices, orthogonal axes, per-row indices and a reversed axis order
+# ---------------------------------------------------------------------------
+
+
+def gen_interp(store: Store):
+    rng = np.random.default_rng(20)
+    sz_x, sz_y = 10, 11
+    k = 0
+
+    def case(a, indices, axis=None, axis_indices=None):
+        nonlocal k
+        name = f"interp_{k}"
+        k += 1
+        store.put(name, "a", a)
+        store.put_tuple(name, "indices", tuple(np.asarray(i) for i in indices))
+        store.set_meta(name, axis=list(axis) if isinstance(axis, tuple) else axis,
+                       axis_indices=list(axis_indices) if isinstance(axis_indices, tuple) else axis_indices)
+        store.put(name, "result", rg.ndarray_linear_interpolation(a, indices, axis=axis, axis_indices=axis_indices))
+
+    a1 = rng.random(sz_x)
+    for x in (np.arange(sz_x), np.linspace(0, sz_x - 1, num=21)):
+        for axis in (None, 0, -1):
+            case(a1, (x,), axis)
+    a2 = rng.random((sz_x, sz_y))
+    for x in (np.arange(sz_x)[:, np.newaxis], np.linspace(0, sz_x - 1, num=100)[:, np.newaxis]):
+        for y in (np.arange(sz_y)[np.newaxis, :], np.linspace(0, sz_y - 1, num=5)[np.newaxis, :]):
+            xb, yb = np.broadcast_arrays(x, y)
+            for axis in (None, (0, 1), (0, ~0)):
+                case(a2, (xb, yb), axis)
+    # extrapolation (clamped cells), negative and beyond the last sample
+    case(a1, (np.linspace(-3.5, sz_x + 2.25, 17),))
+    case(a2, tuple(np.broadcast_arrays(np.linspace(-2, sz_x + 1, 7)[:, None], np.linspace(-1.5, sz_y + 3, 9)[None, :])))
+    # orthogonal axes: a stack of 2D arrays, indices shared (size-1 axis) or per slice
+    a3 = rng.random((9, sz_x, sz_y))
+    case(a3, (rng.uniform(0, sz_x - 1, (1, 20)), rng.uniform(0, sz_y - 1, (1, 20))), axis=(1, 2), axis_indices=1)
+    case(a3, (rng.uniform(0, sz_x - 1, (9, 20)), rng.uniform(0, sz_y - 1, (9, 20))), axis=(-2, -1), axis_indices=-1)
+    # per-row indices along axis 1 of a (9, 10) array, and along axis 0
+    a4 = rng.random((9, sz_x))
+    case(a4, (rng.uniform(-1, sz_x, (9, 15)),), axis=1, axis_indices=1)
+    case(a4, (rng.uniform(0, 8, (1, 15)),), axis=0, axis_indices=1)
+    # the interpolation axes given in reverse order
+    case(a2, tuple(np.broadcast_arrays(rng.uniform(0, sz_x - 1, (6, 1)), rng.uniform(0, sz_y - 1, (1, 4)))),
+         axis=(1, 0))
+    # orthogonal broadcasting of a against the indices
+    a5 = rng.random((1, sz_x, sz_y))
+    case(a5, (rng.uniform(0, sz_x - 1, (3, 7)), rng.uniform(0, sz_y - 1, (3, 7))), axis=(1, 2), axis_indices=1)
+    # integer samples
+    case(np.arange(12).reshape(3, 4) * 3, (np.array([0.25, 1.5, 2.75]), np.array([0.5, 1.0, 2.5])), axis=(0, 1))
+
+
+def main(which=None):
+    if which is None or "known" in which:
+        s = Store()
+        gen_conservative_2d(s)
+        gen_layout_and_seed(s)
+        gen_transposes(s)
+        gen_grids(s)
+        s.save("known_answers.npz")
+    if which is None or "one_dim" in which:
+        s = Store()
+        gen_1d(s)
+        s.save("one_dim.npz")
+    if which is None or "curvilinear" in which:
+        s = Store()
+        gen_curvilinear(s)
+        s.save("curvilinear.npz")
+    if which is None or "interp" in which:
+        s = Store()
+        gen_interp(s)
+        s.save("interp.npz")
 
 
 if __name__ == "__main__":
-    main()
+    # optional arguments: which files to regenerate (known, one_dim, curvilinear, interp)
+    main(sys.argv[1:] or None)

@@ -169,3 +169,17 @@ def test_degenerate_grids_hit_the_step_cap():
     xo, yo = np.meshgrid(b, b, indexing="ij")
     with pytest.raises(RuntimeError, match="status 2"):
         oracle.sweep_2d((xr, yr), (xo, yo))
+
+
+INTERP = fixtures.load("interp.npz")
+
+
+@pytest.mark.parametrize("k", range(27))
+def test_oracle_ndarray_linear_interpolation(k):
+    c = INTERP.case(f"interp_{k}")
+    meta = c.meta
+    axis = tuple(meta["axis"]) if isinstance(meta["axis"], list) else meta["axis"]
+    ai = meta["axis_indices"]
+    ai = tuple(ai) if isinstance(ai, list) else ai
+    got = oracle.ndarray_linear_interpolation(c["a"], c.tuple("indices"), axis=axis, axis_indices=ai)
+    np.testing.assert_array_equal(got, c["result"])

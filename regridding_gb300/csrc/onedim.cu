@@ -506,34 +506,65 @@ __device__ __forceinline__ int64_t interp_cell(double v, int64_t n) {
     return c;
 }
 
+// The per-point part of the upstream formulas: the cell and the weights
+// (1D: w00 = 1 - dx, w10 = dx).  When every element shares the points it is
+// computed once per point and reused for all the elements a thread visits,
+// which halves the FP64 operations per output value (the FP64 pipe, not HBM,
+// bounds this kernel on GB300).
+struct InterpPoint {
+    int64_t i0, j0;
+    double w00, w01, w10, w11;
+};
+
+__device__ __forceinline__ InterpPoint interp_point(double xv, double yv, int64_t nx, int64_t ny) {
+    InterpPoint q;
+    q.i0 = interp_cell(xv, nx);
+    const double dx = dsub(xv, (double)q.i0);
+    if (ny == 0) {
+        q.j0 = 0;
+        q.w00 = dsub(1.0, dx);
+        q.w10 = dx;
+        q.w01 = q.w11 = 0.0;
+    } else {
+        q.j0 = interp_cell(yv, ny);
+        const double dy = dsub(yv, (double)q.j0);
+        q.w00 = dmul(dsub(1.0, dx), dsub(1.0, dy));
+        q.w01 = dmul(dsub(1.0, dx), dy);
+        q.w10 = dmul(dx, dsub(1.0, dy));
+        q.w11 = dmul(dx, dy);
+    }
+    return q;
+}
+
+// a0 * (1 - dx) + a1 * dx (:217), and (a00 * w00) + (a01 * w01) + (a10 * w10)
+// + (a11 * w11) left to right (:268).
+__device__ __forceinline__ double interp_eval(const double* __restrict__ s, const InterpPoint& q, int64_t ny) {
+    if (ny == 0) return dadd(dmul(s[q.i0], q.w00), dmul(s[q.i0 + 1], q.w10));
+    const double* r0 = s + q.i0 * ny + q.j0;
+    const double* r1 = r0 + ny;
+    return dadd(dadd(dadd(dmul(r0[0], q.w00), dmul(r0[1], q.w01)), dmul(r1[0], q.w10)), dmul(r1[1], q.w11));
+}
+
+// Thread = one point p for a run of `run` consecutive elements (grid y);
+// reads of each element's samples by neighbouring threads fall on
+// neighbouring points, and the output rows are written coalesced.
 __global__ void interp_kernel(const double* __restrict__ a, int64_t a_stride, int64_t nx, int64_t ny,
                               const double* __restrict__ x, const double* __restrict__ y, int64_t i_stride,
-                              int64_t m, int64_t n_orth, double* __restrict__ out) {
-    const int64_t total = n_orth * m;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < total;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t e = k / m, p = k - e * m;
-        const double* s = a + e * a_stride;
-        const double xv = x[e * i_stride + p];
-        const int64_t x0 = interp_cell(xv, nx);
-        const double dx = dsub(xv, (double)x0);
-        const int64_t i0 = x0, i1 = x0 + 1;
-        double r;
-        if (ny == 0) {
-            r = dadd(dmul(s[i0], dsub(1.0, dx)), dmul(s[i1], dx));
-        } else {
-            const double yv = y[e * i_stride + p];
-            const int64_t y0 = interp_cell(yv, ny);
-            const double dy = dsub(yv, (double)y0);
-            const int64_t j0 = y0, j1 = y0 + 1;
-            const double w00 = dmul(dsub(1.0, dx), dsub(1.0, dy));
-            const double w01 = dmul(dsub(1.0, dx), dy);
-            const double w10 = dmul(dx, dsub(1.0, dy));
-            const double w11 = dmul(dx, dy);
-            r = dadd(dadd(dadd(dmul(s[i0 * ny + j0], w00), dmul(s[i0 * ny + j1], w01)), dmul(s[i1 * ny + j0], w10)),
-                     dmul(s[i1 * ny + j1], w11));
+                              int64_t m, int64_t n_orth, int64_t run, double* __restrict__ out) {
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < m; p += (int64_t)gridDim.x * blockDim.x) {
+        for (int64_t e0 = blockIdx.y * run; e0 < n_orth; e0 += (int64_t)gridDim.y * run) {
+            const int64_t e1 = e0 + run < n_orth ? e0 + run : n_orth;
+            if (i_stride == 0) {
+                const InterpPoint q = interp_point(x[p], ny ? y[p] : 0.0, nx, ny);
+                for (int64_t e = e0; e < e1; ++e) out[e * m + p] = interp_eval(a + e * a_stride, q, ny);
+            } else {
+                for (int64_t e = e0; e < e1; ++e) {
+                    const int64_t k = e * i_stride + p;
+                    const InterpPoint q = interp_point(x[k], ny ? y[k] : 0.0, nx, ny);
+                    out[e * m + p] = interp_eval(a + e * a_stride, q, ny);
+                }
+            }
         }
-        out[k] = r;
     }
 }
 
@@ -550,10 +581,12 @@ extern "C" int rg_interp_linear(const double* d_a, int64_t a_stride, int64_t nx,
     RG_CHECK(ny == 0 || d_y, RG_ERR_ARG, "rg_interp_linear: 2D interpolation needs y indices");
     if (m == 0 || n_orth == 0) return RG_OK;
     RG_CHECK(d_a && d_x && d_out, RG_ERR_ARG, "rg_interp_linear: NULL argument");
-    const int64_t total = n_orth * m;
-    const unsigned grid = grid_for(total, 256) > 16384 ? 16384 : grid_for(total, 256);
-    interp_kernel<<<grid, 256, 0, (cudaStream_t)stream>>>(d_a, a_stride, nx, ny, d_x, d_y, i_stride, m, n_orth,
-                                                          d_out);
+    const int64_t run = i_stride == 0 ? (n_orth < 16 ? n_orth : 16) : 1;
+    const int64_t runs = (n_orth + run - 1) / run;
+    const unsigned gx = grid_for(m, 256) > (1u << 20) ? (1u << 20) : grid_for(m, 256);
+    const unsigned gy = runs > 65535 ? 65535u : (unsigned)runs;
+    interp_kernel<<<dim3(gx, gy), 256, 0, (cudaStream_t)stream>>>(d_a, a_stride, nx, ny, d_x, d_y, i_stride, m,
+                                                                  n_orth, run, d_out);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
 }

@@ -530,6 +530,10 @@ def run_interp(args, torch):
             "kernel_ms": round(statistics.mean(per) * 1e3, 4),
             "kernel_GB_per_s": round(nbytes / statistics.mean(per) / 1e9, 1),
             "frac_of_measured_hbm": round(nbytes / statistics.mean(per) / 1e9 / peak, 3),
+            # bound: the FP64 pipe (2 operations per clock per SM, 152 SMs): 4 products and 3
+            # sums per value plus the 8-operation weights of a point shared by 16 slices
+            "fp64_ops_per_value": 7.5,
+            "frac_of_fp64_peak_at_2070MHz": round(depth * n * n * 7.5 / statistics.mean(per) / (152 * 2 * 2.07e9), 3),
             "public_call_ms": round(min(ts) * 1e3, 2), "bit_identical_to_oracle": same,
             "cpu_baseline": {"points_per_s": round(n * n / t_cpu, 0), "cores": 1, "kind": "port",
                              "sample": "one 2048^2 slice, numpy"}}

@@ -79,6 +79,8 @@ def _load():
             lib.orc_multilinear_1d.argtypes = [I, I, P, I, I, P, I, P, P, I, P, P, P, P]
             lib.orc_conservative_1d.argtypes = [I, P, I, P, P, I, P, P, P, P]
             lib.orc_conservative_1d.restype = I
+            lib.orc_fill_gauss_seidel_f64.argtypes = [I, I, I, P, P, I]
+            lib.orc_fill_gauss_seidel_f32.argtypes = [I, I, I, P, P, I]
             _lib = lib
     return _lib
 
@@ -322,3 +324,57 @@ def ndarray_linear_interpolation(a, indices, axis=None, axis_indices=None):
             raise NotImplementedError
         result[ii] = r.reshape(idx[0][ii].shape)
     return result
+
+
+# --------------------------------------------------------------------------
+# fill (red-black Gauss-Seidel)
+# --------------------------------------------------------------------------
+
+
+def fill_median_guess(a: np.ndarray, where: np.ndarray, axis: tuple[int, ...]) -> np.ndarray:
+    """``_guess_median`` (regridding/_fill/_gauss_seidel.py:61-80): the
+    median of the valid elements along ``axis``, 0 where there are none."""
+    import warnings
+
+    b = np.where(where, np.nan, a)
+    with warnings.catch_warnings():
+        warnings.simplefilter("ignore", category=RuntimeWarning)
+        med = np.nanmedian(b, axis=axis, keepdims=True)
+    return np.where(np.isnan(med), 0, med)
+
+
+def fill(a, where=None, axis=None, guess=None, num_iterations: int = 100) -> np.ndarray:
+    """``fill(method="gauss_seidel")`` (regridding/_fill/_fill.py:10-109,
+    _gauss_seidel.py:12-58): the host steps in numpy, the sweeps in C
+    (``orc_fill_gauss_seidel_f64``; float32 arrays follow Numba's typing in
+    ``orc_fill_gauss_seidel_f32``)."""
+    if where is None:
+        where = np.isnan(a)
+    a = np.array(a, copy=True)
+    a, where = np.broadcast_arrays(a, where, subok=True)
+    a = np.array(a)
+    ndim = a.ndim
+    axis = tuple(range(ndim)) if axis is None else axis
+    axis = np.lib.array_utils.normalize_axis_tuple(axis, ndim=ndim)
+    axis = tuple(int(v) for v in ~(~np.array(axis) % ndim))
+    if guess is None:
+        guess = fill_median_guess(a, where, axis)
+    a[where] = np.broadcast_to(guess, a.shape)[where]
+    if len(axis) != 2:
+        raise ValueError(f"The number of interpolation axes, {len(axis)},is not supported")
+    dest = (-2, -1)
+    shape_slice = tuple(a.shape[ax] for ax in axis)
+    moved = np.moveaxis(a, axis, dest)
+    shape_moved = moved.shape
+    work = np.ascontiguousarray(moved.reshape(-1, *shape_slice))
+    w = np.ascontiguousarray(np.moveaxis(where, axis, dest).reshape(-1, *shape_slice), dtype=np.uint8)
+    nt, ny, nx = work.shape
+    if num_iterations > 0 and nt > 0 and (nx == 1 or ny == 1):
+        raise ZeroDivisionError("float division by zero")
+    if work.dtype == np.float32:
+        _load().orc_fill_gauss_seidel_f32(nt, ny, nx, _ptr(work), _ptr(w), int(num_iterations))
+    else:
+        work = work.astype(np.float64, copy=False)
+        _load().orc_fill_gauss_seidel_f64(nt, ny, nx, _ptr(work), _ptr(w), int(num_iterations))
+    return np.moveaxis(work.reshape(shape_moved), dest, axis)
+

@@ -756,3 +756,71 @@ int64_t orc_conservative_1d(int64_t nin, const double *xin_raw, int64_t nout, co
     }
     return count;
 }
+
+/* ------------------------------------------------------------------------
+ * Red-black Gauss-Seidel fill: _fill_gauss_seidel_2d and
+ * _iteration_gauss_seidel_2d (regridding/_fill/_gauss_seidel.py:83-139).
+ * a is (nt, ny, nx) C-ordered; only cells with where != 0 are rewritten.
+ * The float64 loop keeps the sequential sweep order (j outer, i inner) and
+ * the periodic neighbours; every operation rounds once.
+ * ------------------------------------------------------------------------ */
+static void gs_constants(int64_t nx, int64_t ny, double *dxxinv, double *dyyinv, double *dcent) {
+    const double dx = 2.0 / (double)(nx - 1);
+    const double dy = 2.0 / (double)(ny - 1);
+    *dxxinv = 1.0 / (dx * dx);
+    *dyyinv = 1.0 / (dy * dy);
+    *dcent = 1.0 / (2.0 * (*dxxinv + *dyyinv));
+}
+
+void orc_fill_gauss_seidel_f64(int64_t nt, int64_t ny, int64_t nx, double *a, const uint8_t *where,
+                               int64_t iterations) {
+    double dxxinv, dyyinv, dcent;
+    gs_constants(nx, ny, &dxxinv, &dyyinv, &dcent);
+    for (int64_t t = 0; t < nt; ++t) {
+        double *s = a + t * ny * nx;
+        const uint8_t *w = where + t * ny * nx;
+        for (int64_t k = 0; k < iterations; ++k) {
+            for (int64_t odd = 0; odd < 2; ++odd) {
+                for (int64_t j = 0; j < ny; ++j) {
+                    for (int64_t i = 0; i < nx; ++i) {
+                        if (((i + j) & 1) != odd || !w[j * nx + i]) continue;
+                        const int64_t i9 = (i - 1 + nx) % nx, i1 = (i + 1) % nx;
+                        const int64_t j9 = (j - 1 + ny) % ny, j1 = (j + 1) % ny;
+                        const double xterm = dxxinv * (s[j * nx + i9] + s[j * nx + i1]);
+                        const double yterm = dyyinv * (s[j9 * nx + i] + s[j1 * nx + i]);
+                        s[j * nx + i] = (xterm + yterm) * dcent;
+                    }
+                }
+            }
+        }
+    }
+}
+
+/* float32 arrays under Numba's typing: the neighbour sums are float32, the
+ * products with the float64 constants and the rest are float64, and the
+ * stored value is rounded to float32. */
+void orc_fill_gauss_seidel_f32(int64_t nt, int64_t ny, int64_t nx, float *a, const uint8_t *where,
+                               int64_t iterations) {
+    double dxxinv, dyyinv, dcent;
+    gs_constants(nx, ny, &dxxinv, &dyyinv, &dcent);
+    for (int64_t t = 0; t < nt; ++t) {
+        float *s = a + t * ny * nx;
+        const uint8_t *w = where + t * ny * nx;
+        for (int64_t k = 0; k < iterations; ++k) {
+            for (int64_t odd = 0; odd < 2; ++odd) {
+                for (int64_t j = 0; j < ny; ++j) {
+                    for (int64_t i = 0; i < nx; ++i) {
+                        if (((i + j) & 1) != odd || !w[j * nx + i]) continue;
+                        const int64_t i9 = (i - 1 + nx) % nx, i1 = (i + 1) % nx;
+                        const int64_t j9 = (j - 1 + ny) % ny, j1 = (j + 1) % ny;
+                        const float sx = s[j * nx + i9] + s[j * nx + i1];
+                        const float sy = s[j9 * nx + i] + s[j1 * nx + i];
+                        const double xterm = dxxinv * (double)sx;
+                        const double yterm = dyyinv * (double)sy;
+                        s[j * nx + i] = (float)((xterm + yterm) * dcent);
+                    }
+                }
+            }
+        }
+    }
+}

@@ -3,7 +3,7 @@
 Run from the repository root (needs the upstream source tree, not available on
 GPU hosts):
 
-    python tests/golden/make_golden.py [known] [one_dim] [curvilinear] [interp]
+    python tests/golden/make_golden.py [known] [one_dim] [curvilinear] [interp] [fill]
 
 The upstream package is imported in its JIT-disabled pure-Python mode through
 ``reference_env`` (the mode its own CI exercises).  Each case below restates
@@ -531,6 +531,71 @@ def gen_interp(store: Store):
     case(np.arange(12).reshape(3, 4) * 3, (np.array([0.25, 1.5, 2.75]), np.array([0.5, 1.0, 2.5])), axis=(0, 1))
 
 
+def gen_fill(store: Store):
+    """regridding.fill (regridding/_fill/_fill.py:10-109): the inputs of the
+    upstream tests (_fill/_fill_test.py:10-119, seeded here), odd and even
+    slice sizes with dense missing sets (the periodic neighbours of the
+    first/last row and column then share the colour of the cell and the
+    sweep order matters), and float64 throughout."""
+    rng = np.random.default_rng(30)
+    k = 0
+
+    def case(a, where, axis, guess=None, num_iterations=11, **extra):
+        nonlocal k
+        name = f"fill_{k}"
+        k += 1
+        store.put(name, "a", a)
+        if where is not None:
+            store.put(name, "where", where)
+        if guess is not None and np.ndim(guess) > 0:
+            store.put(name, "guess", guess)
+            g_meta = "array"
+        else:
+            g_meta = guess
+        store.set_meta(name, axis=list(axis) if isinstance(axis, tuple) else axis, guess=g_meta,
+                       num_iterations=num_iterations, has_where=where is not None, **extra)
+        store.put(name, "result", rg.fill(a, where=where, axis=axis, guess=guess, num_iterations=num_iterations))
+
+    nx, ny, nt = 11, 12, 13
+    # _fill_test.py:10-49
+    for guess in (None, 0.5):
+        case(rng.uniform(0, 1, (nx, ny)), rng.uniform(0, 1, (nx, ny)) > 0.9, None, guess)
+        case(rng.uniform(0, 1, (nt, nx, ny)), rng.uniform(0, 1, (nt, nx, ny)) > 0.9, (~1, ~0), guess)
+        with np.errstate(invalid="ignore"):
+            case(np.sqrt(rng.uniform(-0.1, 1, (nx, nt, ny))), None, (0, ~0), guess)
+    # _fill_test.py:52-79: zero iterations return the guess
+    for guess in (None, 2.0, np.arange(nt, dtype=float).reshape(nt, 1, 1)):
+        case(rng.uniform(0, 1, (nt, nx, ny)), rng.uniform(0, 1, (nt, nx, ny)) > 0.9, (~1, ~0), guess, 0)
+    # _fill_test.py:82-97: a harmonic field with a missing block
+    x = np.linspace(-1, 1, num=32)
+    a = x[:, np.newaxis] + 2 * x[np.newaxis, :]
+    a[10:16, 10:16] = np.nan
+    case(a, None, None, None, 300)
+    # _fill_test.py:100-119: a slice with no valid elements
+    a = rng.uniform(0, 1, (nt, nx, ny))
+    where = rng.uniform(0, 1, a.shape) > 0.9
+    where[0] = True
+    case(a, where, (~1, ~0), None, 11)
+    # odd / even slice sizes, dense missing sets, periodic wrap
+    for shape in ((9, 7), (8, 7), (7, 8), (8, 8), (7, 9), (2, 5), (5, 2), (3, 3)):
+        for frac in (0.5, 0.95):
+            case(rng.uniform(-1, 1, (3,) + shape), rng.uniform(0, 1, (3,) + shape) < frac, (1, 2), None, 7)
+    # all cells missing but one, and a guess array varying over the slice
+    a = rng.uniform(0, 1, (6, 9))
+    where = np.ones(a.shape, dtype=bool)
+    where[2, 3] = False
+    case(a, where, None, rng.uniform(0, 1, (6, 9)), 5)
+    # orthogonal axis in the middle, guess per orthogonal element
+    a = rng.uniform(0, 1, (5, 4, 6))
+    case(a, rng.uniform(0, 1, a.shape) < 0.4, (0, 2), rng.uniform(0, 1, (1, 4, 1)), 9)
+    # where broadcast against a
+    a = rng.uniform(0, 1, (4, 7, 8))
+    case(a, rng.uniform(0, 1, (7, 8)) < 0.3, (1, 2), None, 6)
+    # a 64 x 64 slice pair, 20 iterations (larger sweep)
+    a = rng.uniform(0, 1, (2, 64, 64))
+    case(a, rng.uniform(0, 1, a.shape) < 0.2, (1, 2), None, 20)
+
+
 def main(which=None):
     if which is None or "known" in which:
         s = Store()
@@ -551,8 +616,12 @@ def main(which=None):
         s = Store()
         gen_interp(s)
         s.save("interp.npz")
+    if which is None or "fill" in which:
+        s = Store()
+        gen_fill(s)
+        s.save("fill.npz")
 
 
 if __name__ == "__main__":
-    # optional arguments: which files to regenerate (known, one_dim, curvilinear, interp)
+    # optional arguments: which files to regenerate (known, one_dim, curvilinear, interp, fill)
     main(sys.argv[1:] or None)

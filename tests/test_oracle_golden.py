@@ -183,3 +183,25 @@ def test_oracle_ndarray_linear_interpolation(k):
     ai = tuple(ai) if isinstance(ai, list) else ai
     got = oracle.ndarray_linear_interpolation(c["a"], c.tuple("indices"), axis=axis, axis_indices=ai)
     np.testing.assert_array_equal(got, c["result"])
+
+
+FILL = fixtures.load("fill.npz")
+N_FILL = 31
+
+
+def fill_args(k):
+    """Inputs of fill fixture k: (a, where, axis, guess, num_iterations)."""
+    c = FILL.case(f"fill_{k}")
+    meta = c.meta
+    axis = tuple(meta["axis"]) if isinstance(meta["axis"], list) else meta["axis"]
+    guess = c["guess"] if meta["guess"] == "array" else meta["guess"]
+    where = c["where"] if meta["has_where"] else None
+    return c["a"], where, axis, guess, meta["num_iterations"], c["result"]
+
+
+@pytest.mark.parametrize("k", range(N_FILL))
+def test_oracle_fill(k):
+    a, where, axis, guess, iters, exp = fill_args(k)
+    got = oracle.fill(a, where=where, axis=axis, guess=guess, num_iterations=iters)
+    assert got.shape == exp.shape
+    np.testing.assert_array_equal(got, exp)

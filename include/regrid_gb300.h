@@ -301,6 +301,30 @@ int rg_interp_linear(const double* d_a, int64_t a_stride, int64_t nx, int64_t ny
                      const double* d_y, int64_t i_stride, int64_t m, int64_t n_orth, double* d_out,
                      rg_stream_t stream);
 
+/* fill(method="gauss_seidel"), regridding/_fill/_fill.py:10-109 and
+ * _gauss_seidel.py:12-139, on a stack of nt slices of ny x nx cells
+ * (C-ordered, dtype RG_F32/RG_F64) with the byte mask d_where (1 = missing),
+ * in place: the missing cells are first set to the guess, then relaxed by
+ * `iterations` red-black Gauss-Seidel iterations with periodic neighbours,
+ * bit-identical to the upstream's sequential sweep (float32 arrays follow
+ * Numba's typing: float32 neighbour sums, float64 products).  d_guess holds
+ * one value per slice (RG_FILL_GUESS_SLICE) or per cell (RG_FILL_GUESS_FULL)
+ * in the array's dtype; RG_FILL_GUESS_MEDIAN seeds with the per-slice median
+ * of rg_fill_median.  An axis of length 1 with iterations > 0 is RG_ERR_ARG
+ * (the upstream divides by zero). */
+#define RG_FILL_GUESS_MEDIAN 0
+#define RG_FILL_GUESS_SLICE 1
+#define RG_FILL_GUESS_FULL 2
+int rg_fill_gauss_seidel(void* d_a, int dtype, const uint8_t* d_where, int64_t nt, int64_t ny, int64_t nx,
+                         const void* d_guess, int guess_kind, int64_t iterations, rg_stream_t stream);
+
+/* The median of the valid (not missing, not NaN) cells of each of nt slices
+ * of `slice` cells into d_out (nt values, the array's dtype), 0 for a slice
+ * without valid cells: _guess_median, regridding/_fill/_gauss_seidel.py:61-80
+ * (numpy's nanmedian: the mean of the two middle values for an even count). */
+int rg_fill_median(const void* d_a, int dtype, const uint8_t* d_where, int64_t nt, int64_t slice, void* d_out,
+                   rg_stream_t stream);
+
 /* Device bytes currently held by a handle: the CSR plus whatever state
  * applies have made on first use (float32 weights, tile lists, transposed
  * CSR).  Used by caches that account weights against an HBM budget.  No

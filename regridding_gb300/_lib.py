@@ -21,6 +21,9 @@ RG_ERR_UNSUPPORTED = 5
 
 RG_F32 = 0
 RG_F64 = 1
+RG_FILL_GUESS_MEDIAN = 0
+RG_FILL_GUESS_SLICE = 1
+RG_FILL_GUESS_FULL = 2
 RG_ACC_EXACT = 0
 RG_ACC_FAST = 1
 RG_BOUNDS = {"extrapolate": 0, "nan": 1, "raise": 2}
@@ -36,6 +39,8 @@ SIGNATURES = {
     "rg_build_conservative_2d": [_P, _P, _I, _I, _P, _P, _I, _I, _P, _P, ctypes.POINTER(_P)],
     "rg_set_sweep_chunk": [_I],
     "rg_interp_linear": [_P, _I, _I, _I, _P, _P, _I, _I, _I, _P, _P],
+    "rg_fill_gauss_seidel": [_P, _C, _P, _I, _I, _I, _P, _C, _I, _P],
+    "rg_fill_median": [_P, _C, _P, _I, _I, _P, _P],
     "rg_build_conservative_2d_batch": [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],
     "rg_weights_from_coo": [_P, _P, _P, _I, _I, _I, _P, ctypes.POINTER(_P)],
     "rg_weights_info": [_P, ctypes.POINTER(_I), ctypes.POINTER(_I), ctypes.POINTER(_I)],

@@ -1,0 +1,479 @@
+// fill(method="gauss_seidel"): red-black Gauss-Seidel relaxation of the
+// missing cells of a stack of 2D slices (regridding/_fill/_gauss_seidel.py
+// :12-139), and the per-slice median of the valid cells that seeds it
+// (_guess_median, :61-80).
+//
+// Layout: a stack of nt slices of ny x nx cells, C-ordered, float64 or
+// float32, and a byte mask `where` of the same shape (1 = missing).
+//
+// Relaxation.  The upstream visits, for every slice, iteration and colour
+// (even cells (i + j) & 1 == 0 first, then odd), the cells of that colour in
+// row-major order and replaces each missing one with
+//     (dxxinv * (a[j, i-1] + a[j, i+1]) + dyyinv * (a[j-1, i] + a[j+1, i])) * dcent
+// with periodic neighbours.  Cells of one colour only read cells of the other
+// colour, except across the periodic seam of an odd axis: with nx odd, column
+// nx - 1 has the colour of column 0 in every row, so (j, 0) reads the old
+// (j, nx - 1) and (j, nx - 1) then reads the new (j, 0); likewise rows 0 and
+// ny - 1 for ny odd.  Each colour is therefore split into three phases run in
+// order: cells off the odd seams, cells on exactly one seam (last column or
+// last row), and the last corner.  Cells within a phase never read one
+// another, so one launch updates a phase of every slice at once and the
+// result equals the sequential sweep bit for bit.  The missing cells of each
+// (colour, phase) class are compacted once, in (slice, cell) order, into a
+// list of 64-bit entries (slice << 32 | cell); every iteration is then six
+// gather launches over the lists, and cells that are not missing cost
+// nothing.  Per updated cell: 6 FP64 operations, 4 neighbour reads, 1 write.
+//
+// Median.  A radix select on order-preserving integer keys of the valid,
+// non-NaN values (8-bit digits, most significant first: 8 histogram passes
+// for float64, 4 for float32), then one pass for the element following the
+// lower median; the median is (lo + hi) / 2 in the array's dtype for an even
+// count (numpy's mean of the two middle elements), the middle element for an
+// odd count, and 0 for a slice without valid values.
+#include "common.cuh"
+
+namespace rg {
+namespace {
+
+constexpr int kClasses = 6;  // colour (2) x phase (3)
+constexpr int kClassifyThreads = 256;
+constexpr int kClassifyItems = 16;
+constexpr int64_t kTile = (int64_t)kClassifyThreads * kClassifyItems;
+
+__device__ __forceinline__ int cell_class(uint32_t j, uint32_t i, uint32_t ny, uint32_t nx) {
+    const int colour = (int)((i + j) & 1u);
+    const int phase = (int)((nx & 1u) && i == nx - 1) + (int)((ny & 1u) && j == ny - 1);
+    return colour * 3 + phase;
+}
+
+// class of cell c of slice t, or -1 when it is not missing / past the slice
+__device__ __forceinline__ int missing_class(const uint8_t* __restrict__ where, uint64_t slice_base, uint32_t c,
+                                             uint32_t S, uint32_t ny, uint32_t nx) {
+    if (c >= S || !where[slice_base + c]) return -1;
+    const uint32_t j = c / nx;
+    return cell_class(j, c - j * nx, ny, nx);
+}
+
+// Pass 1: missing cells per (class, tile); counts laid out [class][block]
+// with block = t * tiles + tile.
+__global__ void __launch_bounds__(kClassifyThreads) fill_count(const uint8_t* __restrict__ where, int64_t nt,
+                                                               uint32_t ny, uint32_t nx, int64_t tiles,
+                                                               unsigned* __restrict__ counts) {
+    __shared__ unsigned sc[kClasses];
+    const uint32_t S = ny * nx;
+    const int64_t nblocks = nt * tiles;
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        if (threadIdx.x < kClasses) sc[threadIdx.x] = 0;
+        __syncthreads();
+        unsigned local[kClasses] = {0, 0, 0, 0, 0, 0};
+        const uint64_t base = (uint64_t)t * S;
+        const uint32_t c0 = (uint32_t)(blockIdx.x * kTile);
+        for (int r = 0; r < kClassifyItems; ++r) {
+            const int cls = missing_class(where, base, c0 + r * kClassifyThreads + threadIdx.x, S, ny, nx);
+#pragma unroll
+            for (int k = 0; k < kClasses; ++k) local[k] += cls == k;
+        }
+#pragma unroll
+        for (int k = 0; k < kClasses; ++k)
+            if (local[k]) atomicAdd(&sc[k], local[k]);
+        __syncthreads();
+        if (threadIdx.x < kClasses) counts[threadIdx.x * nblocks + t * tiles + blockIdx.x] = sc[threadIdx.x];
+        __syncthreads();
+    }
+}
+
+// Pass 2: write the entries of every class in (slice, cell) order: warp
+// ballots give each missing cell its rank among the tile's cells of its
+// class, on top of the scanned offset of (class, block).
+__global__ void __launch_bounds__(kClassifyThreads) fill_lists(const uint8_t* __restrict__ where, int64_t nt,
+                                                               uint32_t ny, uint32_t nx, int64_t tiles,
+                                                               const int64_t* __restrict__ offsets,
+                                                               uint64_t* __restrict__ list) {
+    constexpr int kWarps = kClassifyThreads / 32;
+    __shared__ unsigned wc[kWarps][kClasses];
+    __shared__ int64_t run[kClasses];
+    const uint32_t S = ny * nx;
+    const int64_t nblocks = nt * tiles;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        if (threadIdx.x < kClasses) run[threadIdx.x] = offsets[threadIdx.x * nblocks + t * tiles + blockIdx.x];
+        const uint64_t base = (uint64_t)t * S;
+        const uint32_t c0 = (uint32_t)(blockIdx.x * kTile);
+        for (int r = 0; r < kClassifyItems; ++r) {
+            const uint32_t c = c0 + r * kClassifyThreads + threadIdx.x;
+            const int cls = missing_class(where, base, c, S, ny, nx);
+            unsigned mine = 0;
+#pragma unroll
+            for (int k = 0; k < kClasses; ++k) {
+                const unsigned b = __ballot_sync(0xffffffffu, cls == k);
+                if (lane == 0) wc[warp][k] = __popc(b);
+                if (cls == k) mine = __popc(b & lt);
+            }
+            __syncthreads();
+            if (cls >= 0) {
+                int64_t pos = run[cls] + mine;
+                for (int w = 0; w < warp; ++w) pos += wc[w][cls];
+                list[pos] = ((uint64_t)t << 32) | c;
+            }
+            __syncthreads();
+            if (threadIdx.x < kClasses) {
+                unsigned tot = 0;
+                for (int w = 0; w < kWarps; ++w) tot += wc[w][threadIdx.x];
+                run[threadIdx.x] += tot;
+            }
+            __syncthreads();
+        }
+    }
+}
+
+// the start of every class in the scanned offsets, and the total
+__global__ void fill_class_starts(const int64_t* __restrict__ offsets, int64_t nblocks, int64_t* __restrict__ out) {
+    const int k = threadIdx.x;
+    if (k <= kClasses) out[k] = offsets[k * nblocks];
+}
+
+struct GsConst {
+    double dxxinv, dyyinv, dcent;
+};
+
+// _iteration_gauss_seidel_2d (:110-139), float64: every operation rounds once.
+__device__ __forceinline__ double gs_value(double l, double r, double d, double u, const GsConst& k) {
+    return dmul(dadd(dmul(k.dxxinv, dadd(l, r)), dmul(k.dyyinv, dadd(d, u))), k.dcent);
+}
+// float32 arrays under Numba's typing: float32 neighbour sums, float64
+// products and sum, the result rounded to float32 on store.
+__device__ __forceinline__ float gs_value(float l, float r, float d, float u, const GsConst& k) {
+    const double xs = (double)__fadd_rn(l, r), ys = (double)__fadd_rn(d, u);
+    return __double2float_rn(dmul(dadd(dmul(k.dxxinv, xs), dmul(k.dyyinv, ys)), k.dcent));
+}
+
+template <typename T>
+__global__ void fill_update(T* __restrict__ a, const uint64_t* __restrict__ list, int64_t n, uint32_t ny,
+                            uint32_t nx, GsConst k) {
+    const uint64_t S = (uint64_t)ny * nx;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
+        const uint64_t e = list[q];
+        const uint32_t c = (uint32_t)e;
+        T* s = a + (e >> 32) * S;
+        const uint32_t j = c / nx, i = c - j * nx;
+        const uint32_t i9 = i ? i - 1 : nx - 1, i1 = i + 1 == nx ? 0 : i + 1;
+        const uint32_t j9 = j ? j - 1 : ny - 1, j1 = j + 1 == ny ? 0 : j + 1;
+        const T* row = s + (uint64_t)j * nx;
+        s[c] = gs_value(row[i9], row[i1], s[(uint64_t)j9 * nx + i], s[(uint64_t)j1 * nx + i], k);
+    }
+}
+
+// a[where] = guess: one value per slice (kind 1) or one per cell (kind 2)
+template <typename T>
+__global__ void fill_seed(T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
+                          const T* __restrict__ guess, int full) {
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < S; c += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t idx = t * S + c;
+            if (where[idx]) a[idx] = full ? guess[idx] : guess[t];
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// per-slice median
+// ---------------------------------------------------------------------------
+
+template <typename T>
+struct Keys;
+template <>
+struct Keys<double> {
+    using K = unsigned long long;
+    static constexpr int kBits = 64;
+    __device__ static K key(double v) {
+        const K u = (K)__double_as_longlong(v);
+        return (u >> 63) ? ~u : (u | (1ull << 63));
+    }
+    __device__ static double value(K k) {
+        const K u = (k >> 63) ? (k & ~(1ull << 63)) : ~k;
+        return __longlong_as_double((long long)u);
+    }
+    __device__ static double mid(double lo, double hi) { return dmul(dadd(lo, hi), 0.5); }
+};
+template <>
+struct Keys<float> {
+    using K = unsigned;
+    static constexpr int kBits = 32;
+    __device__ static K key(float v) {
+        const K u = (K)__float_as_uint(v);
+        return (u >> 31) ? ~u : (u | (1u << 31));
+    }
+    __device__ static float value(K k) {
+        const K u = (k >> 31) ? (k & ~(1u << 31)) : ~k;
+        return __uint_as_float(u);
+    }
+    __device__ static float mid(float lo, float hi) { return __fmul_rn(__fadd_rn(lo, hi), 0.5f); }
+};
+
+struct MedianState {
+    unsigned long long prefix, mask;  // digits of the lower median's key chosen so far
+    unsigned long long min_gt;        // smallest key above the lower median
+    unsigned long long count_le;      // valid keys <= the lower median
+    long long n, k;                   // valid count, rank still to find within the prefix
+};
+
+// histogram of the next digit over the valid keys matching the prefix
+template <typename T>
+__global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
+                            int shift, const MedianState* __restrict__ st, unsigned* __restrict__ hist) {
+    using KT = Keys<T>;
+    __shared__ unsigned h[256];
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
+        __syncthreads();
+        const unsigned long long prefix = st[t].prefix, mask = st[t].mask;
+        const T* s = a + t * S;
+        const uint8_t* w = where + t * S;
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < S; c += (int64_t)gridDim.x * blockDim.x) {
+            const T v = s[c];
+            if (w[c] || v != v) continue;
+            const unsigned long long key = KT::key(v);
+            if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255u], 1u);
+        }
+        __syncthreads();
+        for (int b = threadIdx.x; b < 256; b += blockDim.x)
+            if (h[b]) atomicAdd(&hist[t * 256 + b], h[b]);
+        __syncthreads();
+    }
+}
+
+// choose the digit holding rank k (first pass: the valid count fixes k)
+__global__ void median_pick(MedianState* __restrict__ st, unsigned* __restrict__ hist, int64_t nt, int shift,
+                            int first) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    unsigned* h = hist + t * 256;
+    MedianState s = st[t];
+    if (first) {
+        long long n = 0;
+        for (int b = 0; b < 256; ++b) n += h[b];
+        s.n = n;
+        s.k = n > 0 ? (n - 1) / 2 : 0;
+    }
+    if (s.n > 0) {
+        long long acc = 0;
+        int b = 0;
+        for (; b < 255; ++b) {
+            if (acc + (long long)h[b] > s.k) break;
+            acc += h[b];
+        }
+        s.k -= acc;
+        s.prefix |= (unsigned long long)b << shift;
+        s.mask |= 255ull << shift;
+    }
+    for (int b = 0; b < 256; ++b) h[b] = 0;
+    st[t] = s;
+}
+
+// valid keys <= the lower median, and the smallest key above it
+template <typename T>
+__global__ void median_upper(const T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
+                             MedianState* __restrict__ st) {
+    using KT = Keys<T>;
+    __shared__ unsigned long long le, gt;
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        if (threadIdx.x == 0) {
+            le = 0;
+            gt = ~0ull;
+        }
+        __syncthreads();
+        const unsigned long long lo = st[t].prefix;
+        unsigned long long my_le = 0, my_gt = ~0ull;
+        const T* s = a + t * S;
+        const uint8_t* w = where + t * S;
+        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < S; c += (int64_t)gridDim.x * blockDim.x) {
+            const T v = s[c];
+            if (w[c] || v != v) continue;
+            const unsigned long long key = KT::key(v);
+            if (key <= lo) ++my_le;
+            else if (key < my_gt) my_gt = key;
+        }
+        if (my_le) atomicAdd(&le, my_le);
+        if (my_gt != ~0ull) atomicMin(&gt, my_gt);
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (le) atomicAdd(&st[t].count_le, le);
+            if (gt != ~0ull) atomicMin(&st[t].min_gt, gt);
+        }
+        __syncthreads();
+    }
+}
+
+template <typename T>
+__global__ void median_write(const MedianState* __restrict__ st, int64_t nt, T* __restrict__ out) {
+    using KT = Keys<T>;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    const MedianState s = st[t];
+    if (s.n == 0) {
+        out[t] = T(0);
+        return;
+    }
+    const T lo = KT::value((typename KT::K)s.prefix);
+    if (s.n & 1) {
+        out[t] = lo;
+        return;
+    }
+    const bool same = s.count_le >= (unsigned long long)(s.n / 2 + 1);
+    out[t] = KT::mid(lo, same ? lo : KT::value((typename KT::K)s.min_gt));
+}
+
+__global__ void median_init(MedianState* __restrict__ st, int64_t nt) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= nt) return;
+    st[t] = MedianState{0ull, 0ull, ~0ull, 0ull, 0, 0};
+}
+
+dim3 slice_grid(int64_t nt, int64_t S, int64_t per_block) {
+    const int64_t ty = nt < 65535 ? nt : 65535;
+    int64_t gx = (S + per_block - 1) / per_block;
+    const int64_t cap = (4 * 152 + ty - 1) / ty;  // about four blocks per SM in all
+    if (gx > cap) gx = cap;
+    if (gx < 1) gx = 1;
+    return dim3((unsigned)gx, (unsigned)(ty < 1 ? 1 : ty));
+}
+
+template <typename T>
+int median_impl(const T* a, const uint8_t* where, int64_t nt, int64_t S, T* out, cudaStream_t s) {
+    MedianState* st = nullptr;
+    unsigned* hist = nullptr;
+    int status = RG_OK;
+    do {
+        if ((status = dalloc(&st, nt, s))) break;
+        if ((status = dalloc(&hist, nt * 256, s))) break;
+        RG_CUDA(cudaMemsetAsync(hist, 0, nt * 256 * sizeof(unsigned), s));
+        const unsigned g1 = grid_for(nt, 256);
+        median_init<<<g1, 256, 0, s>>>(st, nt);
+        const dim3 grid = slice_grid(nt, S, 8192);
+        for (int pass = 0; pass < Keys<T>::kBits / 8; ++pass) {
+            const int shift = Keys<T>::kBits - 8 * (pass + 1);
+            median_hist<T><<<grid, 256, 0, s>>>(a, where, nt, S, shift, st, hist);
+            median_pick<<<g1, 256, 0, s>>>(st, hist, nt, shift, pass == 0);
+        }
+        median_upper<T><<<grid, 256, 0, s>>>(a, where, nt, S, st);
+        median_write<T><<<g1, 256, 0, s>>>(st, nt, out);
+        RG_CUDA(cudaGetLastError());
+    } while (0);
+    dfree(hist, s);
+    dfree(st, s);
+    return status;
+}
+
+GsConst gs_constants(int64_t ny, int64_t nx) {
+    // _iteration_gauss_seidel_2d (:121-129): the domain [-1, 1] on both axes
+    GsConst k;
+    const double dx = 2.0 / (double)(nx - 1);
+    const double dy = 2.0 / (double)(ny - 1);
+    k.dxxinv = 1.0 / (dx * dx);
+    k.dyyinv = 1.0 / (dy * dy);
+    k.dcent = 1.0 / (2.0 * (k.dxxinv + k.dyyinv));
+    return k;
+}
+
+template <typename T>
+int gauss_seidel_impl(T* a, const uint8_t* where, int64_t nt, int64_t ny, int64_t nx, const T* guess, int kind,
+                      int64_t iterations, cudaStream_t s) {
+    const int64_t S = ny * nx;
+    T* med = nullptr;
+    unsigned* counts = nullptr;
+    int64_t* offsets = nullptr;
+    int64_t* starts_dev = nullptr;
+    uint64_t* list = nullptr;
+    int status = RG_OK;
+    do {
+        // seed the missing cells
+        if (kind == RG_FILL_GUESS_MEDIAN) {
+            if ((status = dalloc(&med, nt, s))) break;
+            if ((status = median_impl<T>(a, where, nt, S, med, s))) break;
+            guess = med;
+        }
+        fill_seed<T><<<slice_grid(nt, S, 4096), 256, 0, s>>>(a, where, nt, S, guess, kind == RG_FILL_GUESS_FULL);
+        RG_CUDA(cudaGetLastError());
+        if (iterations == 0) break;
+
+        // compact the missing cells of every (colour, phase) class
+        const int64_t tiles = (S + kTile - 1) / kTile;
+        const int64_t nblocks = nt * tiles;
+        const int64_t ncounts = kClasses * nblocks + 1;
+        if ((status = dalloc(&counts, ncounts, s))) break;
+        if ((status = dalloc(&offsets, ncounts, s))) break;
+        if ((status = dalloc(&starts_dev, kClasses + 1, s))) break;
+        RG_CUDA(cudaMemsetAsync(counts, 0, ncounts * sizeof(unsigned), s));
+        const dim3 cgrid((unsigned)tiles, (unsigned)(nt < 65535 ? nt : 65535));
+        fill_count<<<cgrid, kClassifyThreads, 0, s>>>(where, nt, (uint32_t)ny, (uint32_t)nx, tiles, counts);
+        if ((status = exclusive_scan_u32_to_i64(counts, offsets, ncounts, nullptr, s))) break;
+        fill_class_starts<<<1, 32, 0, s>>>(offsets, nblocks, starts_dev);
+        int64_t starts[kClasses + 1];
+        RG_CUDA(cudaMemcpyAsync(starts, starts_dev, sizeof(starts), cudaMemcpyDeviceToHost, s));
+        RG_CUDA(cudaStreamSynchronize(s));
+        const int64_t total = starts[kClasses];
+        if (total == 0) break;
+        if ((status = dalloc(&list, total, s))) break;
+        fill_lists<<<cgrid, kClassifyThreads, 0, s>>>(where, nt, (uint32_t)ny, (uint32_t)nx, tiles, offsets, list);
+        RG_CUDA(cudaGetLastError());
+
+        // relax: per iteration and colour, the phases in order
+        const GsConst k = gs_constants(ny, nx);
+        for (int64_t it = 0; it < iterations; ++it) {
+            for (int cls = 0; cls < kClasses; ++cls) {
+                const int64_t n = starts[cls + 1] - starts[cls];
+                if (n == 0) continue;
+                unsigned g = grid_for(n, 256);
+                if (g > 152u * 16u) g = 152u * 16u;
+                fill_update<T><<<g, 256, 0, s>>>(a, list + starts[cls], n, (uint32_t)ny, (uint32_t)nx, k);
+            }
+        }
+        RG_CUDA(cudaGetLastError());
+    } while (0);
+    dfree(list, s);
+    dfree(starts_dev, s);
+    dfree(offsets, s);
+    dfree(counts, s);
+    dfree(med, s);
+    return status;
+}
+
+}  // namespace
+}  // namespace rg
+
+extern "C" int rg_fill_median(const void* d_a, int dtype, const uint8_t* d_where, int64_t nt, int64_t slice,
+                              void* d_out, rg_stream_t stream) {
+    using namespace rg;
+    RG_CHECK(dtype == RG_F32 || dtype == RG_F64, RG_ERR_ARG, "rg_fill_median: dtype must be RG_F32 or RG_F64");
+    RG_CHECK(nt >= 0 && slice >= 0, RG_ERR_ARG, "rg_fill_median: negative size");
+    if (nt == 0) return RG_OK;
+    RG_CHECK(d_out && (slice == 0 || (d_a && d_where)), RG_ERR_ARG, "rg_fill_median: NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (dtype == RG_F64) return median_impl<double>((const double*)d_a, d_where, nt, slice, (double*)d_out, s);
+    return median_impl<float>((const float*)d_a, d_where, nt, slice, (float*)d_out, s);
+}
+
+extern "C" int rg_fill_gauss_seidel(void* d_a, int dtype, const uint8_t* d_where, int64_t nt, int64_t ny, int64_t nx,
+                                    const void* d_guess, int guess_kind, int64_t iterations, rg_stream_t stream) {
+    using namespace rg;
+    RG_CHECK(dtype == RG_F32 || dtype == RG_F64, RG_ERR_ARG,
+             "rg_fill_gauss_seidel: dtype must be RG_F32 or RG_F64");
+    RG_CHECK(nt >= 0 && ny >= 0 && nx >= 0 && iterations >= 0, RG_ERR_ARG, "rg_fill_gauss_seidel: negative size");
+    RG_CHECK(guess_kind == RG_FILL_GUESS_MEDIAN || guess_kind == RG_FILL_GUESS_SLICE ||
+                 guess_kind == RG_FILL_GUESS_FULL,
+             RG_ERR_ARG, "rg_fill_gauss_seidel: unknown guess kind %d", guess_kind);
+    RG_CHECK(nt < (1ll << 31) && ny * nx < (1ll << 31), RG_ERR_ARG,
+             "rg_fill_gauss_seidel: at most 2^31 slices of fewer than 2^31 cells");
+    if (nt == 0 || ny * nx == 0) return RG_OK;
+    RG_CHECK(iterations == 0 || (nx >= 2 && ny >= 2), RG_ERR_ARG,
+             "rg_fill_gauss_seidel: division by zero (an axis of length 1)");
+    RG_CHECK(d_a && d_where && (guess_kind == RG_FILL_GUESS_MEDIAN || d_guess), RG_ERR_ARG,
+             "rg_fill_gauss_seidel: NULL argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    if (dtype == RG_F64)
+        return gauss_seidel_impl<double>((double*)d_a, d_where, nt, ny, nx, (const double*)d_guess, guess_kind,
+                                         iterations, s);
+    return gauss_seidel_impl<float>((float*)d_a, d_where, nt, ny, nx, (const float*)d_guess, guess_kind, iterations,
+                                    s);
+}

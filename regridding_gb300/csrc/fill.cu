@@ -218,23 +218,34 @@ struct MedianState {
     long long n, k;                   // valid count, rank still to find within the prefix
 };
 
-// histogram of the next digit over the valid keys matching the prefix
+// histogram of the next digit over the valid keys matching the prefix; the
+// lanes of a warp that share a bin add to it once (the leading digits of
+// real data fall into a few bins, where per-lane atomics would serialise)
 template <typename T>
 __global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
                             int shift, const MedianState* __restrict__ st, unsigned* __restrict__ hist) {
     using KT = Keys<T>;
     __shared__ unsigned h[256];
+    const unsigned lane = threadIdx.x & 31u;
     for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
         for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
         __syncthreads();
         const unsigned long long prefix = st[t].prefix, mask = st[t].mask;
         const T* s = a + t * S;
         const uint8_t* w = where + t * S;
-        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < S; c += (int64_t)gridDim.x * blockDim.x) {
-            const T v = s[c];
-            if (w[c] || v != v) continue;
-            const unsigned long long key = KT::key(v);
-            if ((key & mask) == prefix) atomicAdd(&h[(key >> shift) & 255u], 1u);
+        // the trip count is uniform over the block, so whole warps take part
+        for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < S; base += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t c = base + threadIdx.x;
+            unsigned bin = 0xffffffffu;
+            if (c < S) {
+                const T v = s[c];
+                if (!w[c] && v == v) {
+                    const unsigned long long key = KT::key(v);
+                    if ((key & mask) == prefix) bin = (unsigned)(key >> shift) & 255u;
+                }
+            }
+            const unsigned peers = __match_any_sync(0xffffffffu, bin);
+            if (bin != 0xffffffffu && (unsigned)(__ffs(peers) - 1) == lane) atomicAdd(&h[bin], __popc(peers));
         }
         __syncthreads();
         for (int b = threadIdx.x; b < 256; b += blockDim.x)

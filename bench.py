@@ -493,7 +493,7 @@ def run_interp(args, torch):
     import regridding_gb300 as rg
     from regridding_gb300 import _device, _lib
 
-    n, depth = 2048, 16
+    n, depth = 2048, (4 if getattr(args, "small", False) else 16)
     g = torch.Generator(device="cuda")
     g.manual_seed(15)
     a = torch.rand((depth, n, n), generator=g, device="cuda", dtype=torch.float64)
@@ -526,14 +526,15 @@ def run_interp(args, torch):
     same = bool(np.array_equal(res[:1], exp0) and np.array_equal(res[-1:], exp_last)
                 and np.array_equal(out[0].cpu().numpy(), exp0.reshape(-1)))
     del a, out, dx, dy
-    return {"workload": "bilinear interpolation, 16 x 2048^2 float64 samples at 2048^2 rotated points",
+    return {"workload": f"bilinear interpolation, {depth} x 2048^2 float64 samples at 2048^2 rotated points",
             "kernel_ms": round(statistics.mean(per) * 1e3, 4),
             "kernel_GB_per_s": round(nbytes / statistics.mean(per) / 1e9, 1),
             "frac_of_measured_hbm": round(nbytes / statistics.mean(per) / 1e9 / peak, 3),
             # bound: the FP64 pipe (2 operations per clock per SM, 152 SMs): 4 products and 3
-            # sums per value plus the 8-operation weights of a point shared by 16 slices
-            "fp64_ops_per_value": 7.5,
-            "frac_of_fp64_peak_at_2070MHz": round(depth * n * n * 7.5 / statistics.mean(per) / (152 * 2 * 2.07e9), 3),
+            # sums per value plus the 8-operation weights of a point shared by all slices
+            "fp64_ops_per_value": 7 + 8 / depth,
+            "frac_of_fp64_peak_at_2070MHz": round(depth * n * n * (7 + 8 / depth) / statistics.mean(per)
+                                                  / (152 * 2 * 2.07e9), 3),
             "public_call_ms": round(min(ts) * 1e3, 2), "bit_identical_to_oracle": same,
             "cpu_baseline": {"points_per_s": round(n * n / t_cpu, 0), "cores": 1, "kind": "port",
                              "sample": "one 2048^2 slice, numpy"}}
@@ -552,6 +553,8 @@ def run_fill(args, torch):
 
     rng = np.random.default_rng(40)
     nt, ny, nx, iters = 64, 1024, 1024, 100
+    if getattr(args, "small", False):
+        nt, iters = 16, 3
     a = rng.normal(0, 1, (nt, ny, nx))
     where = np.zeros(a.shape, bool)
     for t in range(nt):
@@ -578,14 +581,15 @@ def run_fill(args, torch):
     _, d_out = run(iters)
     per_iter = (t_full - t_seed) / iters
     t0 = time.perf_counter()
-    res = rg.fill(a, where=where, axis=(1, 2))
+    res = rg.fill(a, where=where, axis=(1, 2), num_iterations=iters)
     t_public = time.perf_counter() - t0
     t0 = time.perf_counter()
-    exp0 = oracle.fill(a[:1], where=where[:1], axis=(1, 2))
+    exp0 = oracle.fill(a[:1], where=where[:1], axis=(1, 2), num_iterations=iters)
     t_cpu = time.perf_counter() - t0
     same = bool(np.array_equal(res[:1], exp0) and np.array_equal(d_out[0].cpu().numpy(), exp0[0]))
     del d_a0, d_w, d_out
-    return {"workload": "fill, 64 x 1024^2 float64, 8.4 % missing in rectangular holes, median guess, 100 iterations",
+    return {"workload": f"fill, {nt} x 1024^2 float64, {100 * missing / where.size:.1f} % missing in rectangular "
+                        f"holes, median guess, {iters} iterations",
             "missing_cells": missing, "device_ms": round(t_full * 1e3, 2),
             "median_and_seed_ms": round(t_seed * 1e3, 2), "iteration_us": round(per_iter * 1e6, 1),
             "cell_updates_per_s": round(missing * iters / (t_full - t_seed), 0),
@@ -593,7 +597,7 @@ def run_fill(args, torch):
             "frac_of_fp64_peak_at_2070MHz": round(missing * 6 / per_iter / (152 * 2 * 2.07e9), 3),
             "public_call_ms": round(t_public * 1e3, 1), "bit_identical_to_oracle_slice": same,
             "cpu_baseline": {"cell_updates_per_s": round(int(where[0].sum()) * iters / t_cpu, 0), "cores": 1,
-                             "kind": "port", "sample": "one 1024^2 slice, 100 iterations, sequential C"}}
+                             "kind": "port", "sample": f"one 1024^2 slice, {iters} iterations, sequential C"}}
 
 
 def run_differentiable(args, torch):
@@ -882,6 +886,16 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+LEGS = {
+    "multilinear_1d": lambda args, torch: run_multilinear_1d(args, torch),
+    "conservative_1d": lambda args, torch: run_conservative_1d(args, torch),
+    "batched": lambda args, torch: run_batched(args, torch),
+    "differentiable": lambda args, torch: run_differentiable(args, torch),
+    "interp_2d": lambda args, torch: run_interp(args, torch),
+    "fill": lambda args, torch: run_fill(args, torch),
+}
+
+
 def main(argv=None):
     p = argparse.ArgumentParser(description=__doc__, formatter_class=argparse.RawDescriptionHelpFormatter)
     p.add_argument("--gpus", type=int, default=1)
@@ -898,6 +912,8 @@ def main(argv=None):
     p.add_argument("--serve-slots", type=int, default=16)
     p.add_argument("--serve-cobuild", type=int, default=0, help="small grids built together per build job")
     p.add_argument("--no-extra", action="store_true", help="skip the differentiable-regrid and batched legs")
+    p.add_argument("--only", choices=sorted(LEGS), help="run one secondary leg alone and print its JSON (profiling)")
+    p.add_argument("--small", action="store_true", help="with --only: the leg's reduced profiling size")
     args = p.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3
@@ -908,6 +924,12 @@ def main(argv=None):
         return
     if args.quick:
         run_quick(args, local)
+        return
+    if args.only:
+        import torch
+
+        torch.cuda.set_device(local)
+        print(json.dumps({args.only: LEGS[args.only](args, torch)}), flush=True)
         return
     if world > 1:
         import torch

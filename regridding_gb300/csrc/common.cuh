@@ -96,6 +96,27 @@ void dfree(T* p, cudaStream_t s) {
     if (p) cudaFreeAsync((void*)p, s);
 }
 
+// Unsigned 32-bit division by a divisor fixed for a launch, as a multiply
+// and two shifts (Granlund and Montgomery, "Division by invariant integers
+// using multiplication", PLDI 1994, figure 4.1): exact for every dividend
+// and every divisor 1 <= d < 2^31, and it keeps the division's reciprocal
+// and correction sequence off the kernel's critical path.
+struct FastDiv {
+    uint32_t d, m, s1, s2;
+    FastDiv() = default;
+    explicit FastDiv(uint32_t div) : d(div) {
+        uint32_t l = 0;
+        while (l < 32 && (1ull << l) < div) ++l;  // ceil(log2 d)
+        m = (uint32_t)((((1ull << 32) * ((1ull << l) - div)) / div) + 1);
+        s1 = l < 1 ? l : 1;
+        s2 = l > 1 ? l - 1 : 0;
+    }
+    __device__ __forceinline__ uint32_t div(uint32_t n) const {
+        const uint32_t t1 = __umulhi(m, n);
+        return (t1 + ((n - t1) >> s1)) >> s2;
+    }
+};
+
 inline unsigned grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;

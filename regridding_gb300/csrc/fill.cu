@@ -148,19 +148,38 @@ __device__ __forceinline__ float gs_value(float l, float r, float d, float u, co
     return __double2float_rn(dmul(dadd(dmul(k.dxxinv, xs), dmul(k.dyyinv, ys)), k.dcent));
 }
 
+// Two list entries per thread, all eight neighbour loads issued before either
+// store: cells of one class never read one another, so the order is free,
+// and the extra loads in flight hide the gather latency.
 template <typename T>
 __global__ void fill_update(T* __restrict__ a, const uint64_t* __restrict__ list, int64_t n, uint32_t ny,
-                            uint32_t nx, GsConst k) {
+                            FastDiv nx_div, GsConst k) {
+    const uint32_t nx = nx_div.d;
     const uint64_t S = (uint64_t)ny * nx;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += (int64_t)gridDim.x * blockDim.x) {
-        const uint64_t e = list[q];
-        const uint32_t c = (uint32_t)e;
-        T* s = a + (e >> 32) * S;
-        const uint32_t j = c / nx, i = c - j * nx;
-        const uint32_t i9 = i ? i - 1 : nx - 1, i1 = i + 1 == nx ? 0 : i + 1;
-        const uint32_t j9 = j ? j - 1 : ny - 1, j1 = j + 1 == ny ? 0 : j + 1;
-        const T* row = s + (uint64_t)j * nx;
-        s[c] = gs_value(row[i9], row[i1], s[(uint64_t)j9 * nx + i], s[(uint64_t)j1 * nx + i], k);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += 2 * stride) {
+        T v[2][4];
+        T* dst[2] = {nullptr, nullptr};
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            const int64_t qq = q + h * stride;
+            if (qq >= n) break;
+            const uint64_t e = list[qq];
+            const uint32_t c = (uint32_t)e;
+            T* s = a + (e >> 32) * S;
+            const uint32_t j = nx_div.div(c), i = c - j * nx;
+            const uint32_t i9 = i ? i - 1 : nx - 1, i1 = i + 1 == nx ? 0 : i + 1;
+            const uint32_t j9 = j ? j - 1 : ny - 1, j1 = j + 1 == ny ? 0 : j + 1;
+            const T* row = s + (uint64_t)j * nx;
+            v[h][0] = row[i9];
+            v[h][1] = row[i1];
+            v[h][2] = s[(uint64_t)j9 * nx + i];
+            v[h][3] = s[(uint64_t)j1 * nx + i];
+            dst[h] = s + c;
+        }
+#pragma unroll
+        for (int h = 0; h < 2; ++h)
+            if (dst[h]) *dst[h] = gs_value(v[h][0], v[h][1], v[h][2], v[h][3], k);
     }
 }
 
@@ -195,6 +214,10 @@ struct Keys<double> {
         return __longlong_as_double((long long)u);
     }
     __device__ static double mid(double lo, double hi) { return dmul(dadd(lo, hi), 0.5); }
+    // NaN test on the bits: keeps the FP64 pipe (2 lanes per clock per SM) out of the scans
+    __device__ static bool is_nan(double v) {
+        return ((unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull) > 0x7ff0000000000000ull;
+    }
 };
 template <>
 struct Keys<float> {
@@ -209,6 +232,7 @@ struct Keys<float> {
         return __uint_as_float(u);
     }
     __device__ static float mid(float lo, float hi) { return __fmul_rn(__fadd_rn(lo, hi), 0.5f); }
+    __device__ static bool is_nan(float v) { return (__float_as_uint(v) & 0x7fffffffu) > 0x7f800000u; }
 };
 
 struct MedianState {
@@ -217,6 +241,10 @@ struct MedianState {
     unsigned long long count_le;      // valid keys <= the lower median
     long long n, k;                   // valid count, rank still to find within the prefix
 };
+
+// Values read per thread before they are used, so that enough loads are in
+// flight to stream the stack at HBM speed.
+constexpr int kMedianUnroll = 8;
 
 // histogram of the next digit over the valid keys matching the prefix; the
 // lanes of a warp that share a bin add to it once (the leading digits of
@@ -227,6 +255,7 @@ __global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__
     using KT = Keys<T>;
     __shared__ unsigned h[256];
     const unsigned lane = threadIdx.x & 31u;
+    const int64_t span = (int64_t)blockDim.x * kMedianUnroll;
     for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
         for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
         __syncthreads();
@@ -234,18 +263,31 @@ __global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__
         const T* s = a + t * S;
         const uint8_t* w = where + t * S;
         // the trip count is uniform over the block, so whole warps take part
-        for (int64_t base = blockIdx.x * (int64_t)blockDim.x; base < S; base += (int64_t)gridDim.x * blockDim.x) {
-            const int64_t c = base + threadIdx.x;
-            unsigned bin = 0xffffffffu;
-            if (c < S) {
-                const T v = s[c];
-                if (!w[c] && v == v) {
-                    const unsigned long long key = KT::key(v);
-                    if ((key & mask) == prefix) bin = (unsigned)(key >> shift) & 255u;
+        for (int64_t base = blockIdx.x * span; base < S; base += (int64_t)gridDim.x * span) {
+            T v[kMedianUnroll];
+            bool ok[kMedianUnroll];
+#pragma unroll
+            for (int u = 0; u < kMedianUnroll; ++u) {
+                const int64_t c = base + u * (int64_t)blockDim.x + threadIdx.x;
+                ok[u] = c < S;
+                if (ok[u]) {
+                    v[u] = s[c];
+                    ok[u] = !w[c];
                 }
             }
-            const unsigned peers = __match_any_sync(0xffffffffu, bin);
-            if (bin != 0xffffffffu && (unsigned)(__ffs(peers) - 1) == lane) atomicAdd(&h[bin], __popc(peers));
+#pragma unroll
+            for (int u = 0; u < kMedianUnroll; ++u) {
+                unsigned bin = 0xffffffffu;
+                if (ok[u] && !KT::is_nan(v[u])) {
+                    const unsigned long long key = KT::key(v[u]);
+                    if ((key & mask) == prefix) bin = (unsigned)(key >> shift) & 255u;
+                }
+                // after the leading digits few keys still match the prefix:
+                // most warps skip the (slow) match entirely
+                if (!__any_sync(0xffffffffu, bin != 0xffffffffu)) continue;
+                const unsigned peers = __match_any_sync(0xffffffffu, bin);
+                if (bin != 0xffffffffu && (unsigned)(__ffs(peers) - 1) == lane) atomicAdd(&h[bin], __popc(peers));
+            }
         }
         __syncthreads();
         for (int b = threadIdx.x; b < 256; b += blockDim.x)
@@ -288,6 +330,7 @@ __global__ void median_upper(const T* __restrict__ a, const uint8_t* __restrict_
                              MedianState* __restrict__ st) {
     using KT = Keys<T>;
     __shared__ unsigned long long le, gt;
+    const int64_t span = (int64_t)blockDim.x * kMedianUnroll;
     for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
         if (threadIdx.x == 0) {
             le = 0;
@@ -298,12 +341,25 @@ __global__ void median_upper(const T* __restrict__ a, const uint8_t* __restrict_
         unsigned long long my_le = 0, my_gt = ~0ull;
         const T* s = a + t * S;
         const uint8_t* w = where + t * S;
-        for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < S; c += (int64_t)gridDim.x * blockDim.x) {
-            const T v = s[c];
-            if (w[c] || v != v) continue;
-            const unsigned long long key = KT::key(v);
-            if (key <= lo) ++my_le;
-            else if (key < my_gt) my_gt = key;
+        for (int64_t base = blockIdx.x * span; base < S; base += (int64_t)gridDim.x * span) {
+            T v[kMedianUnroll];
+            bool ok[kMedianUnroll];
+#pragma unroll
+            for (int u = 0; u < kMedianUnroll; ++u) {
+                const int64_t c = base + u * (int64_t)blockDim.x + threadIdx.x;
+                ok[u] = c < S;
+                if (ok[u]) {
+                    v[u] = s[c];
+                    ok[u] = !w[c];
+                }
+            }
+#pragma unroll
+            for (int u = 0; u < kMedianUnroll; ++u) {
+                if (!ok[u] || KT::is_nan(v[u])) continue;
+                const unsigned long long key = KT::key(v[u]);
+                if (key <= lo) ++my_le;
+                else if (key < my_gt) my_gt = key;
+            }
         }
         if (my_le) atomicAdd(&le, my_le);
         if (my_gt != ~0ull) atomicMin(&gt, my_gt);
@@ -344,7 +400,7 @@ __global__ void median_init(MedianState* __restrict__ st, int64_t nt) {
 dim3 slice_grid(int64_t nt, int64_t S, int64_t per_block) {
     const int64_t ty = nt < 65535 ? nt : 65535;
     int64_t gx = (S + per_block - 1) / per_block;
-    const int64_t cap = (4 * 152 + ty - 1) / ty;  // about four blocks per SM in all
+    const int64_t cap = (6 * 152 + ty - 1) / ty;  // one wave of six 256-thread blocks per SM in all
     if (gx > cap) gx = cap;
     if (gx < 1) gx = 1;
     return dim3((unsigned)gx, (unsigned)(ty < 1 ? 1 : ty));
@@ -429,15 +485,22 @@ int gauss_seidel_impl(T* a, const uint8_t* where, int64_t nt, int64_t ny, int64_
         fill_lists<<<cgrid, kClassifyThreads, 0, s>>>(where, nt, (uint32_t)ny, (uint32_t)nx, tiles, offsets, list);
         RG_CUDA(cudaGetLastError());
 
-        // relax: per iteration and colour, the phases in order
+        // relax: per iteration and colour, the phases in order; each launch
+        // is one wave of resident blocks walking its list
         const GsConst k = gs_constants(ny, nx);
+        int dev = 0, sms = 0, per_sm = 0;
+        RG_CUDA(cudaGetDevice(&dev));
+        RG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
+        RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, fill_update<T>, 256, 0));
+        const int64_t wave = (int64_t)sms * (per_sm > 0 ? per_sm : 1);
+        const FastDiv nx_div((uint32_t)nx);
         for (int64_t it = 0; it < iterations; ++it) {
             for (int cls = 0; cls < kClasses; ++cls) {
                 const int64_t n = starts[cls + 1] - starts[cls];
                 if (n == 0) continue;
-                unsigned g = grid_for(n, 256);
-                if (g > 152u * 16u) g = 152u * 16u;
-                fill_update<T><<<g, 256, 0, s>>>(a, list + starts[cls], n, (uint32_t)ny, (uint32_t)nx, k);
+                const int64_t need = (n + 511) / 512;  // two entries per thread
+                const unsigned g = (unsigned)(need < wave ? need : wave);
+                fill_update<T><<<g, 256, 0, s>>>(a, list + starts[cls], n, (uint32_t)ny, nx_div, k);
             }
         }
         RG_CUDA(cudaGetLastError());

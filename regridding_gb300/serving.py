@@ -210,6 +210,7 @@ class _Request:
     future: Future
     t_arrival: float
     result: object = None
+    grids_hashed: bool = False  # key = grid_key(grids) + (perturb, seed)
     t_start: float = 0.0  # its job started on a slot
     t_built: float = 0.0  # its weights were ready (build jobs)
     t_done: float = 0.0
@@ -236,11 +237,17 @@ class GpuBackend:
     # 2048^2 -> 1536^2 build: about 220 B per cell)
     BUILD_BYTES_PER_CELL = 256
 
-    def __init__(self, accumulate: str = "fast", perturb: bool = True, seed: int = 42):
+    def __init__(self, accumulate: str = "fast", perturb: bool = True, seed: int = 42, disk_cache=None):
         self.torch = _device.torch()
         self.accumulate = accumulate
         self.perturb = perturb
         self.seed = seed
+        # weights files shared with store.WeightsDiskCache.weights(..., method="conservative")
+        self.disk = disk_cache
+        self.disk_loads = 0
+        self._disk_stream = self.torch.cuda.Stream() if disk_cache is not None else None
+        self._writer = ThreadPoolExecutor(max_workers=1, thread_name_prefix="regrid-disk") \
+            if disk_cache is not None else None
 
     def grids(self, grid_input, grid_output):
         """The coordinates a build sees: the output jittered as the upstream
@@ -304,14 +311,74 @@ class GpuBackend:
     def build_bytes(self, req: _Request) -> int:
         return self.BUILD_BYTES_PER_CELL * (req.n_in + req.n_out)
 
+    def disk_key(self, req: _Request) -> str | None:
+        """Name of the request's weights in the disk cache: the grid hashes
+        of its serving key, with the build's perturbation and seed."""
+        from . import store
+
+        grids = req.key[:-2] if req.grids_hashed else None
+        return store.weights_key(tuple(req.grid_input), tuple(req.grid_output), method="conservative",
+                                 perturb=self.perturb, seed=self.seed, grids=grids)
+
+    def _footprint(self, dw) -> int:
+        nbytes = ctypes.c_int64()
+        _lib.call("rg_weights_device_bytes", dw.handle, ctypes.byref(nbytes))
+        # room for the float32 weights and tile lists the first apply makes
+        return nbytes.value + dw.nnz * 6 + (dw.n_out // 32 + 1) * 16
+
     def build(self, slot, req: _Request):
+        dkey = self.disk_key(req) if self.disk is not None else None
+        if dkey is not None:
+            stored = self.disk.get(dkey)
+            if stored is not None:
+                ii, oo, vv = stored[0].reshape(-1)[0]
+                xo = req.grid_output[0]
+                with self.torch.cuda.stream(slot.stream):
+                    dw = _device.DeviceWeights.from_coo(ii, oo, vv, req.n_in, req.n_out,
+                                                        (xo.shape[0] - 1, xo.shape[1] - 1))
+                self.disk_loads += 1
+                return dw, self._footprint(dw)
         gi, go = self.grids(req.grid_input, req.grid_output)
         with self.torch.cuda.stream(slot.stream):
             dw = _device.build_conservative_2d(gi, go)
-            nbytes = ctypes.c_int64()
-            _lib.call("rg_weights_device_bytes", dw.handle, ctypes.byref(nbytes))
-            # room for the float32 weights and tile lists the first apply makes
-            return dw, nbytes.value + dw.nnz * 6 + (dw.n_out // 32 + 1) * 16
+        if dkey is not None:
+            self._persist(slot, dkey, dw, np.shape(req.grid_input[0]), np.shape(req.grid_output[0]))
+        return dw, self._footprint(dw)
+
+    def _persist(self, slot, key: str, dw, shape_in, shape_out) -> None:
+        """Export the new weights on the slot's stream, copy them to pinned
+        host memory on a side stream, and write the file from the writer
+        thread once the copy is done (the slot goes on meanwhile)."""
+        t = self.torch
+        with t.cuda.stream(slot.stream):
+            dev = dw.export()
+            exported = t.cuda.Event()
+            exported.record(slot.stream)
+        side = self._disk_stream
+        side.wait_event(exported)
+        with t.cuda.stream(side):
+            host = []
+            for d in dev:
+                d.record_stream(side)
+                h = t.empty(d.shape, dtype=d.dtype, pin_memory=True)
+                h.copy_(d, non_blocking=True)
+                host.append(h)
+            copied = t.cuda.Event()
+            copied.record(side)
+
+        def write():
+            copied.synchronize()
+            array = np.empty((), dtype=object)
+            array[()] = tuple(h.numpy() for h in host)
+            self.disk.put(key, (array, tuple(shape_in), tuple(shape_out)), {"method": "conservative"})
+            del dev[:]
+
+        self._writer.submit(write)
+
+    def flush(self) -> None:
+        """Wait for the weights files still being written."""
+        if self._writer is not None:
+            self._writer.submit(lambda: None).result()
 
     def build_many(self, slot, reqs: list) -> list:
         """Weights of several grid pairs in one batched build: per request
@@ -392,15 +459,21 @@ class RegridServer:
         (their requests then find the weights cached).  Small builds are
         dominated by fixed per-build costs that a batch pays once; large
         builds gain little and would make the small ones wait.
+    disk_cache:
+        A :class:`~regridding_gb300.store.WeightsDiskCache`: a build first
+        looks for the weights file of its grid pair there (an upload instead
+        of a build), and new weights are written to it in the background.
+        The files are those of ``disk_cache.weights(grid_input, grid_output,
+        method="conservative")``, so servers and batch jobs share them.
     """
 
     def __init__(self, hbm_budget: float = 80e9, slots: int = 4, cache_bytes: float | None = None,
                  max_batch_stack: int = 64, accumulate: str = "fast", perturb: bool = True, seed: int = 42,
                  intake_threads: int = 4, max_cobuild: int = 0, cobuild_max_cells: int = 512 * 512,
-                 backend=None):
+                 backend=None, disk_cache=None):
         if accumulate not in ("fast", "exact"):
             raise ValueError(f"accumulate must be 'fast' or 'exact', got {accumulate!r}")
-        self.backend = backend if backend is not None else GpuBackend(accumulate, perturb, seed)
+        self.backend = backend if backend is not None else GpuBackend(accumulate, perturb, seed, disk_cache)
         self._key_extra = (bool(perturb), int(seed))
         self.budget = int(hbm_budget)
         self.cache = WeightsLRU(int(cache_bytes if cache_bytes is not None else hbm_budget // 2),
@@ -466,6 +539,7 @@ class RegridServer:
     def _key_and_queue(self, req: _Request) -> None:
         try:
             req.key = grid_key(req.grid_input, req.grid_output) + self._key_extra
+            req.grids_hashed = True
         except Exception as e:  # noqa: BLE001
             req.future.set_exception(e)
             with self._cv:

@@ -82,13 +82,16 @@ class DeviceWeights:
     :func:`regridding_gb300.weights`; applied with :meth:`apply`.
     """
 
-    def __init__(self, handle: ctypes.c_void_p, shape_out: tuple[int, ...] | None = None):
+    def __init__(self, handle: ctypes.c_void_p, shape_out: tuple[int, ...] | None = None,
+                 shape_in: tuple[int, ...] | None = None):
         self._h = handle
         nnz, n_in, n_out = ctypes.c_int64(), ctypes.c_int64(), ctypes.c_int64()
         _lib.call("rg_weights_info", handle, ctypes.byref(nnz), ctypes.byref(n_in), ctypes.byref(n_out))
         self.nnz, self.n_in, self.n_out = nnz.value, n_in.value, n_out.value
         if shape_out is not None and len(shape_out) == 2 and shape_out[0] * shape_out[1] == self.n_out:
             _lib.call("rg_weights_set_output_shape", handle, int(shape_out[0]), int(shape_out[1]))
+        if shape_in is not None and len(shape_in) == 2 and shape_in[0] * shape_in[1] == self.n_in:
+            _lib.call("rg_weights_set_input_shape", handle, int(shape_in[0]), int(shape_in[1]))
         self._finalizer = weakref.finalize(self, _free_handle, handle.value)
 
     @property
@@ -97,8 +100,11 @@ class DeviceWeights:
 
     @classmethod
     def from_coo(cls, indices_input, indices_output, values, n_in: int, n_out: int,
-                 shape_out: tuple[int, ...] | None = None) -> "DeviceWeights":
-        """Upload entries in the saved layout (numpy or CUDA tensors)."""
+                 shape_out: tuple[int, ...] | None = None,
+                 shape_in: tuple[int, ...] | None = None) -> "DeviceWeights":
+        """Upload entries in the saved layout (numpy or CUDA tensors).  The
+        2D shapes of the output and input cells, when given, let the fast
+        apply tile rows and stage input boxes as for built weights."""
         t = torch()
         ii = _as_device(indices_input, t.int64)
         oo = _as_device(indices_output, t.int64)
@@ -106,7 +112,7 @@ class DeviceWeights:
         h = ctypes.c_void_p()
         _lib.call("rg_weights_from_coo", ptr(ii), ptr(oo), ptr(vv), int(vv.numel()), int(n_in), int(n_out),
                   stream(), ctypes.byref(h))
-        return cls(h, shape_out)
+        return cls(h, shape_out, shape_in)
 
     def export(self):
         """Entries in the saved layout, sorted by (input, output), as CUDA tensors."""

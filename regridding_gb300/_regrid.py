@@ -125,7 +125,7 @@ def regrid_from_weights(
             ii, oo, vv = element
             vv = getattr(vv, "value", vv)
             dw = _device.DeviceWeights.from_coo(np.asarray(ii), np.asarray(oo), np.asarray(vv, dtype=np.float64),
-                                                n_in, n_out, shape_out_numba)
+                                                n_in, n_out, shape_out_numba, shape_in_numba)
             _device.remember(element, dw)
         if d_all is not None:
             src = d_all

@@ -332,10 +332,11 @@ class GpuBackend:
             stored = self.disk.get(dkey)
             if stored is not None:
                 ii, oo, vv = stored[0].reshape(-1)[0]
-                xo = req.grid_output[0]
+                xi, xo = req.grid_input[0], req.grid_output[0]
                 with self.torch.cuda.stream(slot.stream):
                     dw = _device.DeviceWeights.from_coo(ii, oo, vv, req.n_in, req.n_out,
-                                                        (xo.shape[0] - 1, xo.shape[1] - 1))
+                                                        (xo.shape[0] - 1, xo.shape[1] - 1),
+                                                        (xi.shape[0] - 1, xi.shape[1] - 1))
                 self.disk_loads += 1
                 return dw, self._footprint(dw)
         gi, go = self.grids(req.grid_input, req.grid_output)

@@ -237,18 +237,34 @@ struct Keys<float> {
 
 struct MedianState {
     unsigned long long prefix, mask;  // digits of the lower median's key chosen so far
-    unsigned long long min_gt;        // smallest key above the lower median
-    unsigned long long count_le;      // valid keys <= the lower median
+    unsigned long long min_above;     // smallest valid key above the candidate range
+    unsigned long long min_gt;        // smallest candidate key above the lower median
+    unsigned long long count_le;      // candidate keys <= the lower median
     long long n, k;                   // valid count, rank still to find within the prefix
+    long long below;                  // valid keys below the candidate range
+    long long cand;                   // valid keys within it (the candidates)
 };
+
+// The two leading digits are chosen from histograms over the whole stack;
+// the keys that share them (a small fraction of real data) are then copied
+// out and the remaining digits are chosen from histograms of those copies.
+constexpr int kDataPasses = 2;
 
 // Values read per thread before they are used, so that enough loads are in
 // flight to stream the stack at HBM speed.
 constexpr int kMedianUnroll = 8;
 
-// histogram of the next digit over the valid keys matching the prefix; the
-// lanes of a warp that share a bin add to it once (the leading digits of
-// real data fall into a few bins, where per-lane atomics would serialise)
+// add `bin` (0xffffffff: nothing) to the block histogram; the lanes of a
+// warp that share a bin add to it once (the leading digits of real data fall
+// into a few bins, where per-lane atomics would serialise)
+__device__ __forceinline__ void hist_add(unsigned* h, unsigned bin, unsigned lane) {
+    if (!__any_sync(0xffffffffu, bin != 0xffffffffu)) return;
+    const unsigned peers = __match_any_sync(0xffffffffu, bin);
+    if (bin != 0xffffffffu && (unsigned)(__ffs(peers) - 1) == lane) atomicAdd(&h[bin], __popc(peers));
+}
+
+// histogram of the next digit over the valid keys of the stack that match
+// the prefix
 template <typename T>
 __global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
                             int shift, const MedianState* __restrict__ st, unsigned* __restrict__ hist) {
@@ -282,11 +298,7 @@ __global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__
                     const unsigned long long key = KT::key(v[u]);
                     if ((key & mask) == prefix) bin = (unsigned)(key >> shift) & 255u;
                 }
-                // after the leading digits few keys still match the prefix:
-                // most warps skip the (slow) match entirely
-                if (!__any_sync(0xffffffffu, bin != 0xffffffffu)) continue;
-                const unsigned peers = __match_any_sync(0xffffffffu, bin);
-                if (bin != 0xffffffffu && (unsigned)(__ffs(peers) - 1) == lane) atomicAdd(&h[bin], __popc(peers));
+                hist_add(h, bin, lane);
             }
         }
         __syncthreads();
@@ -296,52 +308,110 @@ __global__ void median_hist(const T* __restrict__ a, const uint8_t* __restrict__
     }
 }
 
-// choose the digit holding rank k (first pass: the valid count fixes k)
-__global__ void median_pick(MedianState* __restrict__ st, unsigned* __restrict__ hist, int64_t nt, int shift,
-                            int first) {
-    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (t >= nt) return;
-    unsigned* h = hist + t * 256;
-    MedianState s = st[t];
-    if (first) {
-        long long n = 0;
-        for (int b = 0; b < 256; ++b) n += h[b];
-        s.n = n;
-        s.k = n > 0 ? (n - 1) / 2 : 0;
-    }
-    if (s.n > 0) {
-        long long acc = 0;
-        int b = 0;
-        for (; b < 255; ++b) {
-            if (acc + (long long)h[b] > s.k) break;
-            acc += h[b];
+// the same over the copied candidate keys of each slice
+__global__ void median_hist_keys(const unsigned long long* __restrict__ keys, const int64_t* __restrict__ offsets,
+                                 int64_t nt, int shift, const MedianState* __restrict__ st,
+                                 unsigned* __restrict__ hist) {
+    __shared__ unsigned h[256];
+    const unsigned lane = threadIdx.x & 31u;
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        for (int b = threadIdx.x; b < 256; b += blockDim.x) h[b] = 0;
+        __syncthreads();
+        const unsigned long long prefix = st[t].prefix, mask = st[t].mask;
+        const int64_t lo = offsets[t], hi = offsets[t + 1];
+        for (int64_t base = lo + blockIdx.x * (int64_t)blockDim.x; base < hi; base += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t c = base + threadIdx.x;
+            unsigned bin = 0xffffffffu;
+            if (c < hi) {
+                const unsigned long long key = keys[c];
+                if ((key & mask) == prefix) bin = (unsigned)(key >> shift) & 255u;
+            }
+            hist_add(h, bin, lane);
         }
-        s.k -= acc;
-        s.prefix |= (unsigned long long)b << shift;
-        s.mask |= 255ull << shift;
+        __syncthreads();
+        for (int b = threadIdx.x; b < 256; b += blockDim.x)
+            if (h[b]) atomicAdd(&hist[t * 256 + b], h[b]);
+        __syncthreads();
     }
-    for (int b = 0; b < 256; ++b) h[b] = 0;
+}
+
+// One warp per slice chooses the digit holding rank k (the first pass
+// counts the valid keys, which fixes k) and clears the histogram.
+__global__ void median_pick(MedianState* __restrict__ st, unsigned* __restrict__ hist, int64_t nt, int shift,
+                            int pass) {
+    const int64_t t = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    const unsigned lane = threadIdx.x & 31u;
+    if (t >= nt) return;  // whole warps
+    unsigned* h = hist + t * 256 + lane * 8;
+    unsigned c[8];
+    long long mine = 0;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+        c[q] = h[q];
+        mine += c[q];
+        h[q] = 0;
+    }
+    long long incl = mine;
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+        const long long up = __shfl_up_sync(0xffffffffu, incl, d);
+        if (lane >= (unsigned)d) incl += up;
+    }
+    const long long total = __shfl_sync(0xffffffffu, incl, 31);
+    MedianState s = st[t];
+    if (pass == 0) {
+        s.n = total;
+        s.k = total > 0 ? (total - 1) / 2 : 0;
+    }
+    if (s.n == 0) {
+        if (lane == 0 && pass == 0) st[t] = s;
+        return;
+    }
+    const long long excl = incl - mine;
+    const unsigned owner = __ffs(__ballot_sync(0xffffffffu, excl <= s.k && s.k < incl)) - 1;
+    if (lane != owner) return;
+    long long acc = excl;
+    int q = 0;
+    for (; q < 7; ++q) {
+        if (acc + (long long)c[q] > s.k) break;
+        acc += c[q];
+    }
+    const int b = (int)lane * 8 + q;
+    s.k -= acc;
+    if (pass < kDataPasses) s.below += acc;
+    s.cand = c[q];
+    s.prefix |= (unsigned long long)b << shift;
+    s.mask |= 255ull << shift;
     st[t] = s;
 }
 
-// valid keys <= the lower median, and the smallest key above it
+__global__ void median_cand_counts(const MedianState* __restrict__ st, int64_t nt, int64_t* __restrict__ counts) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t < nt) counts[t] = st[t].n > 0 ? st[t].cand : 0;
+    if (t == nt) counts[t] = 0;
+}
+
+// copy the valid keys within the candidate range (warp-aggregated slots)
+// and find the smallest valid key above it
 template <typename T>
-__global__ void median_upper(const T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
-                             MedianState* __restrict__ st) {
+__global__ void median_compact(const T* __restrict__ a, const uint8_t* __restrict__ where, int64_t nt, int64_t S,
+                               MedianState* __restrict__ st, const int64_t* __restrict__ offsets,
+                               unsigned long long* __restrict__ cursor, unsigned long long* __restrict__ keys) {
     using KT = Keys<T>;
-    __shared__ unsigned long long le, gt;
+    __shared__ unsigned long long above;
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned lt = (1u << lane) - 1u;
     const int64_t span = (int64_t)blockDim.x * kMedianUnroll;
     for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
-        if (threadIdx.x == 0) {
-            le = 0;
-            gt = ~0ull;
-        }
+        if (threadIdx.x == 0) above = ~0ull;
         __syncthreads();
-        const unsigned long long lo = st[t].prefix;
-        unsigned long long my_le = 0, my_gt = ~0ull;
+        const unsigned long long prefix = st[t].prefix, mask = st[t].mask;
+        const bool any = st[t].n > 0;
+        const int64_t out0 = offsets[t];
+        unsigned long long my_above = ~0ull;
         const T* s = a + t * S;
         const uint8_t* w = where + t * S;
-        for (int64_t base = blockIdx.x * span; base < S; base += (int64_t)gridDim.x * span) {
+        for (int64_t base = blockIdx.x * span; any && base < S; base += (int64_t)gridDim.x * span) {
             T v[kMedianUnroll];
             bool ok[kMedianUnroll];
 #pragma unroll
@@ -355,11 +425,47 @@ __global__ void median_upper(const T* __restrict__ a, const uint8_t* __restrict_
             }
 #pragma unroll
             for (int u = 0; u < kMedianUnroll; ++u) {
-                if (!ok[u] || KT::is_nan(v[u])) continue;
-                const unsigned long long key = KT::key(v[u]);
-                if (key <= lo) ++my_le;
-                else if (key < my_gt) my_gt = key;
+                bool in = false;
+                unsigned long long key = 0;
+                if (ok[u] && !KT::is_nan(v[u])) {
+                    key = KT::key(v[u]);
+                    in = (key & mask) == prefix;
+                    if (!in && key > prefix && key < my_above) my_above = key;
+                }
+                const unsigned m = __ballot_sync(0xffffffffu, in);
+                if (m) {
+                    const unsigned leader = __ffs(m) - 1;
+                    unsigned long long slot = 0;
+                    if (lane == leader) slot = atomicAdd(&cursor[t], (unsigned long long)__popc(m));
+                    slot = __shfl_sync(0xffffffffu, slot, leader);
+                    if (in) keys[out0 + slot + __popc(m & lt)] = key;
+                }
             }
+        }
+        if (my_above != ~0ull) atomicMin(&above, my_above);
+        __syncthreads();
+        if (threadIdx.x == 0 && above != ~0ull) atomicMin(&st[t].min_above, above);
+        __syncthreads();
+    }
+}
+
+// candidates <= the lower median, and the smallest candidate above it
+__global__ void median_upper_keys(const unsigned long long* __restrict__ keys, const int64_t* __restrict__ offsets,
+                                  int64_t nt, MedianState* __restrict__ st) {
+    __shared__ unsigned long long le, gt;
+    for (int64_t t = blockIdx.y; t < nt; t += gridDim.y) {
+        if (threadIdx.x == 0) {
+            le = 0;
+            gt = ~0ull;
+        }
+        __syncthreads();
+        const unsigned long long lo = st[t].prefix;
+        unsigned long long my_le = 0, my_gt = ~0ull;
+        for (int64_t c = offsets[t] + blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < offsets[t + 1];
+             c += (int64_t)gridDim.x * blockDim.x) {
+            const unsigned long long key = keys[c];
+            if (key <= lo) ++my_le;
+            else if (key < my_gt) my_gt = key;
         }
         if (my_le) atomicAdd(&le, my_le);
         if (my_gt != ~0ull) atomicMin(&gt, my_gt);
@@ -387,14 +493,17 @@ __global__ void median_write(const MedianState* __restrict__ st, int64_t nt, T* 
         out[t] = lo;
         return;
     }
-    const bool same = s.count_le >= (unsigned long long)(s.n / 2 + 1);
-    out[t] = KT::mid(lo, same ? lo : KT::value((typename KT::K)s.min_gt));
+    // the element after the lower median: itself when it repeats, else the
+    // next candidate, else the first key above the candidate range
+    const bool same = (unsigned long long)s.below + s.count_le >= (unsigned long long)(s.n / 2 + 1);
+    const unsigned long long next = s.min_gt != ~0ull ? s.min_gt : s.min_above;
+    out[t] = KT::mid(lo, same ? lo : KT::value((typename KT::K)next));
 }
 
 __global__ void median_init(MedianState* __restrict__ st, int64_t nt) {
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (t >= nt) return;
-    st[t] = MedianState{0ull, 0ull, ~0ull, 0ull, 0, 0};
+    st[t] = MedianState{0ull, 0ull, ~0ull, ~0ull, 0ull, 0, 0, 0, 0};
 }
 
 dim3 slice_grid(int64_t nt, int64_t S, int64_t per_block) {
@@ -410,23 +519,52 @@ template <typename T>
 int median_impl(const T* a, const uint8_t* where, int64_t nt, int64_t S, T* out, cudaStream_t s) {
     MedianState* st = nullptr;
     unsigned* hist = nullptr;
+    int64_t* counts = nullptr;
+    int64_t* offsets = nullptr;
+    unsigned long long* cursor = nullptr;
+    unsigned long long* keys = nullptr;
     int status = RG_OK;
     do {
         if ((status = dalloc(&st, nt, s))) break;
         if ((status = dalloc(&hist, nt * 256, s))) break;
+        if ((status = dalloc(&counts, nt + 1, s))) break;
+        if ((status = dalloc(&offsets, nt + 1, s))) break;
+        if ((status = dalloc(&cursor, nt, s))) break;
         RG_CUDA(cudaMemsetAsync(hist, 0, nt * 256 * sizeof(unsigned), s));
+        RG_CUDA(cudaMemsetAsync(cursor, 0, nt * sizeof(unsigned long long), s));
         const unsigned g1 = grid_for(nt, 256);
+        const unsigned gw = grid_for(nt * 32, 256);  // a warp per slice
         median_init<<<g1, 256, 0, s>>>(st, nt);
         const dim3 grid = slice_grid(nt, S, 8192);
-        for (int pass = 0; pass < Keys<T>::kBits / 8; ++pass) {
+        constexpr int kPasses = Keys<T>::kBits / 8;
+        for (int pass = 0; pass < kDataPasses; ++pass) {
             const int shift = Keys<T>::kBits - 8 * (pass + 1);
             median_hist<T><<<grid, 256, 0, s>>>(a, where, nt, S, shift, st, hist);
-            median_pick<<<g1, 256, 0, s>>>(st, hist, nt, shift, pass == 0);
+            median_pick<<<gw, 256, 0, s>>>(st, hist, nt, shift, pass);
         }
-        median_upper<T><<<grid, 256, 0, s>>>(a, where, nt, S, st);
+        // copy out the candidates (one host synchronisation for their count)
+        median_cand_counts<<<grid_for(nt + 1, 256), 256, 0, s>>>(st, nt, counts);
+        if ((status = exclusive_scan_i64(counts, offsets, nt + 1, nullptr, s))) break;
+        int64_t total = 0;
+        RG_CUDA(cudaMemcpyAsync(&total, offsets + nt, sizeof(total), cudaMemcpyDeviceToHost, s));
+        RG_CUDA(cudaStreamSynchronize(s));
+        if ((status = dalloc(&keys, total > 0 ? total : 1, s))) break;
+        median_compact<T><<<grid, 256, 0, s>>>(a, where, nt, S, st, offsets, cursor, keys);
+        const int64_t per_slice = (total + nt - 1) / (nt > 0 ? nt : 1);
+        const dim3 kgrid = slice_grid(nt, per_slice, 4096);
+        for (int pass = kDataPasses; pass < kPasses; ++pass) {
+            const int shift = Keys<T>::kBits - 8 * (pass + 1);
+            median_hist_keys<<<kgrid, 256, 0, s>>>(keys, offsets, nt, shift, st, hist);
+            median_pick<<<gw, 256, 0, s>>>(st, hist, nt, shift, pass);
+        }
+        median_upper_keys<<<kgrid, 256, 0, s>>>(keys, offsets, nt, st);
         median_write<T><<<g1, 256, 0, s>>>(st, nt, out);
         RG_CUDA(cudaGetLastError());
     } while (0);
+    dfree(keys, s);
+    dfree(cursor, s);
+    dfree(offsets, s);
+    dfree(counts, s);
     dfree(hist, s);
     dfree(st, s);
     return status;

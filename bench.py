@@ -253,7 +253,8 @@ def run_serving(args, torch):
         # a fresh server per pass: the 32 resident grids are built before the
         # stream starts, every new grid of the stream is built during it
         with RegridServer(hbm_budget=80e9, slots=args.serve_slots, max_batch_stack=64, perturb=False,
-                          max_cobuild=args.serve_cobuild) as srv:
+                          max_cobuild=args.serve_cobuild, urgent_builds=args.serve_urgent,
+                          switch_interval=args.serve_switch_ms / 1e3 if args.serve_switch_ms else None) as srv:
             warm = [srv.submit(gi, go, np.zeros((1, cells(gi)), np.float32)) for gi, go in cached]
             for f in warm:
                 f.result()
@@ -893,6 +894,7 @@ LEGS = {
     "differentiable": lambda args, torch: run_differentiable(args, torch),
     "interp_2d": lambda args, torch: run_interp(args, torch),
     "fill": lambda args, torch: run_fill(args, torch),
+    "serving": lambda args, torch: run_serving(args, torch),
 }
 
 
@@ -911,6 +913,8 @@ def main(argv=None):
     p.add_argument("--serve-requests", type=int, default=1000, help="requests of the served stream (0: skip)")
     p.add_argument("--serve-slots", type=int, default=16)
     p.add_argument("--serve-cobuild", type=int, default=0, help="small grids built together per build job")
+    p.add_argument("--serve-urgent", type=int, default=0, help="1: build jobs on high-priority streams")
+    p.add_argument("--serve-switch-ms", type=float, default=0.0, help="GIL switch interval (0: unchanged)")
     p.add_argument("--no-extra", action="store_true", help="skip the differentiable-regrid and batched legs")
     p.add_argument("--only", choices=sorted(LEGS), help="run one secondary leg alone and print its JSON (profiling)")
     p.add_argument("--small", action="store_true", help="with --only: the leg's reduced profiling size")

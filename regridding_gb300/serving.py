@@ -34,6 +34,7 @@ from __future__ import annotations
 
 import collections
 import ctypes
+import sys
 import threading
 import time
 import weakref
@@ -237,9 +238,11 @@ class GpuBackend:
     # 2048^2 -> 1536^2 build: about 220 B per cell)
     BUILD_BYTES_PER_CELL = 256
 
-    def __init__(self, accumulate: str = "fast", perturb: bool = True, seed: int = 42, disk_cache=None):
+    def __init__(self, accumulate: str = "fast", perturb: bool = True, seed: int = 42, disk_cache=None,
+                 urgent_builds: bool = False):
         self.torch = _device.torch()
         self.accumulate = accumulate
+        self.urgent_builds = urgent_builds
         self.perturb = perturb
         self.seed = seed
         # weights files shared with store.WeightsDiskCache.weights(..., method="conservative")
@@ -259,14 +262,23 @@ class GpuBackend:
         return gi, go
 
     class Slot:
-        """A slot's compute stream and the stream its input copies use."""
+        """A slot's compute stream and the stream its input copies use; with
+        ``urgent`` also a high-priority stream for the jobs that build (the
+        work on the critical path of the slowest requests)."""
 
-        def __init__(self, torch):
+        def __init__(self, torch, urgent: bool = False):
             self.stream = torch.cuda.Stream()
             self.copy = torch.cuda.Stream()
+            self.urgent = None
+            if urgent:
+                view = GpuBackend.Slot.__new__(GpuBackend.Slot)
+                view.stream = torch.cuda.Stream(priority=-1)
+                view.copy = self.copy
+                view.urgent = None
+                self.urgent = view
 
     def make_slot(self, index: int):
-        return GpuBackend.Slot(self.torch)
+        return GpuBackend.Slot(self.torch, self.urgent_builds)
 
     def stage(self, slot, requests: list):
         """Start copying the requests' stacks to one device buffer on the
@@ -460,6 +472,12 @@ class RegridServer:
         (their requests then find the weights cached).  Small builds are
         dominated by fixed per-build costs that a batch pays once; large
         builds gain little and would make the small ones wait.
+    urgent_builds:
+        Run the jobs that build on high-priority CUDA streams, so that the
+        block scheduler serves them before the applies of resident grids.
+    switch_interval:
+        If given, ``sys.setswitchinterval`` for the process: how long a
+        thread may hold the GIL before another runnable thread gets it.
     disk_cache:
         A :class:`~regridding_gb300.store.WeightsDiskCache`: a build first
         looks for the weights file of its grid pair there (an upload instead
@@ -471,10 +489,16 @@ class RegridServer:
     def __init__(self, hbm_budget: float = 80e9, slots: int = 4, cache_bytes: float | None = None,
                  max_batch_stack: int = 64, accumulate: str = "fast", perturb: bool = True, seed: int = 42,
                  intake_threads: int = 4, max_cobuild: int = 0, cobuild_max_cells: int = 512 * 512,
-                 backend=None, disk_cache=None):
+                 backend=None, disk_cache=None, urgent_builds: bool = False,
+                 switch_interval: float | None = None):
         if accumulate not in ("fast", "exact"):
             raise ValueError(f"accumulate must be 'fast' or 'exact', got {accumulate!r}")
-        self.backend = backend if backend is not None else GpuBackend(accumulate, perturb, seed, disk_cache)
+        if switch_interval is not None:
+            # the interpreter's thread switch interval bounds how long a slot
+            # thread back from a native call waits for the GIL (process-wide)
+            sys.setswitchinterval(switch_interval)
+        self.backend = backend if backend is not None else GpuBackend(accumulate, perturb, seed, disk_cache,
+                                                                      urgent_builds)
         self._key_extra = (bool(perturb), int(seed))
         self.budget = int(hbm_budget)
         self.cache = WeightsLRU(int(cache_bytes if cache_bytes is not None else hbm_budget // 2),
@@ -701,6 +725,8 @@ class RegridServer:
 
     def _run(self, slot: int, stream, job: _Job) -> None:
         job.t_start = time.perf_counter()
+        if job.build and getattr(stream, "urgent", None) is not None:
+            stream = stream.urgent
         err = None
         built = False
         cobuild = job.cobuild or []

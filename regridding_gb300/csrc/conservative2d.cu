@@ -279,19 +279,30 @@ __global__ void bbox_partial(const double* __restrict__ x, const double* __restr
     if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = s[threadIdx.x][0];
 }
 
+// one warp: each lane folds a stride of the partials, then a shuffle tree
 __global__ void bbox_combine(const double* __restrict__ part, int nparts, double* __restrict__ out4) {
-    if (threadIdx.x != 0) return;
+    const int lane = threadIdx.x & 31;
+    if (threadIdx.x >= 32) return;
     double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
-    for (int k = 0; k < nparts; k++) {
+    for (int k = lane; k < nparts; k += 32) {
         a = fmin(a, part[4 * k]);
         b = fmin(b, part[4 * k + 1]);
         c = fmax(c, part[4 * k + 2]);
         d = fmax(d, part[4 * k + 3]);
     }
-    out4[0] = a;
-    out4[1] = b;
-    out4[2] = c;
-    out4[3] = d;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
+        c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+        d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    }
+    if (lane == 0) {
+        out4[0] = a;
+        out4[1] = b;
+        out4[2] = c;
+        out4[3] = d;
+    }
 }
 
 // Boundary polygon of grid_boundary (_grids.py:167-215), vertex k.
@@ -1141,6 +1152,9 @@ int locate_2d_exact(const double* x, const double* y, int64_t nx, int64_t ny, co
 }
 
 std::atomic<int64_t> g_sweep_chunk{32};
+// the walk kernel keeps 8 blocks of 64 threads per SM: 152 x 512 threads
+constexpr int64_t kTargetChunks = 152 * 512;
+constexpr int64_t kMinChunk = 4;
 
 namespace {
 
@@ -1211,7 +1225,20 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
     // sweep segments per chunk: rg_set_sweep_chunk (default 32), the
     // RG_SWEEP_CHUNK environment variable overriding it (0 walks whole lines)
     int64_t ch = g_sweep_chunk.load();
-    if (const char* env = getenv("RG_SWEEP_CHUNK")) ch = atoll(env);
+    if (const char* env = getenv("RG_SWEEP_CHUNK")) {
+        ch = atoll(env);
+    } else if (ch > kMinChunk) {
+        // Small batches: shorter chunks, so that the walk still has about
+        // kTargetChunks threads (each chunk is one thread's sequential walk;
+        // a 128^2 pair in chunks of 32 segments keeps 2,000 threads busy
+        // for 0.7 ms).  Every chunk length gives the same triples in the
+        // same order.
+        int64_t segments = 0;
+        for (int g = 0; g < G; g++)
+            for (int f = 0; f < 4; f++) segments += P[g].fam[f].lines * (P[g].fam[f].len - 1);
+        const int64_t fit = (segments + kTargetChunks - 1) / kTargetChunks;
+        ch = std::min<int64_t>(ch, std::max<int64_t>(kMinChunk, fit));
+    }
     *nraw_out = -1;
     if (ch <= 0) return RG_OK;
     std::vector<ChunkPlan> C((size_t)G);

@@ -39,7 +39,10 @@ def ptr(t) -> ctypes.c_void_p | None:
 
 
 def upload(a: np.ndarray, dtype=None):
-    """Host array -> contiguous CUDA tensor (pinned staging for large arrays)."""
+    """Host array -> contiguous CUDA tensor, copied straight from the
+    array's (pageable) memory: on the Grace host of a GB300 that runs at
+    110-160 GB/s for arrays of 8-34 MB, twice the rate of staging through a
+    pinned copy first (whose host memcpy runs at 15-25 GB/s)."""
     t = torch()
     a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
     if a.dtype == np.bool_:
@@ -48,9 +51,6 @@ def upload(a: np.ndarray, dtype=None):
         # read-only arrays (the saved weights) are only read from
         warnings.simplefilter("ignore", UserWarning)
         host = t.from_numpy(a)
-    if a.nbytes >= (1 << 20):
-        host = host.pin_memory()
-        return host.to("cuda", non_blocking=True)
     return host.to("cuda")
 
 

@@ -44,27 +44,84 @@ namespace {
 // geometry (regridding/geometry.py)
 // ---------------------------------------------------------------------------
 
-// bounding_boxes_intersect_2d: geometry.py:153-284
+// Order-preserving integer image of a double for the comparisons below:
+// keys compare (signed) as the doubles do, -0.0 and +0.0 share a key, and
+// NaN is handled by the caller.  Integer compares keep the walk's many
+// bounding-box tests off the FP64 pipe (2 lanes per clock per SM on GB300).
+__device__ __forceinline__ long long order_key(double v) {
+    const long long b = __double_as_longlong(v);
+    if ((b & 0x7fffffffffffffffll) == 0) return 0;
+    return b ^ ((b >> 63) & 0x7fffffffffffffffll);
+}
+
+__device__ __forceinline__ bool any_nan(double a, double b, double c, double d) {
+    const unsigned long long m = 0x7fffffffffffffffull, inf = 0x7ff0000000000000ull;
+    return (((unsigned long long)__double_as_longlong(a) & m) > inf) |
+           (((unsigned long long)__double_as_longlong(b) & m) > inf) |
+           (((unsigned long long)__double_as_longlong(c) & m) > inf) |
+           (((unsigned long long)__double_as_longlong(d) & m) > inf);
+}
+
+// bounding_boxes_intersect_2d: geometry.py:153-284.  The upstream orders
+// each pair and compares min/max; any NaN coordinate makes one of its
+// comparisons false, so NaN means no intersection here too.
 __device__ __forceinline__ bool bboxes_intersect(double xp1, double yp1, double xp2, double yp2,
                                                  double xq1, double yq1, double xq2, double yq2) {
-    double t;
-    if (xp1 > xp2) { t = xp1; xp1 = xp2; xp2 = t; }
-    if (xq1 > xq2) { t = xq1; xq1 = xq2; xq2 = t; }
-    if (!(xp1 <= xq2 && xq1 <= xp2)) return false;
-    if (yp1 > yp2) { t = yp1; yp1 = yp2; yp2 = t; }
-    if (yq1 > yq2) { t = yq1; yq1 = yq2; yq2 = t; }
-    if (!(yp1 <= yq2 && yq1 <= yp2)) return false;
-    return true;
+    if (any_nan(xp1, xp2, xq1, xq2) || any_nan(yp1, yp2, yq1, yq2)) return false;
+    long long a = order_key(xp1), b = order_key(xp2), c = order_key(xq1), d = order_key(xq2);
+    if (!(min(a, b) <= max(c, d) && min(c, d) <= max(a, b))) return false;
+    a = order_key(yp1), b = order_key(yp2), c = order_key(yq1), d = order_key(yq2);
+    return min(a, b) <= max(c, d) && min(c, d) <= max(a, b);
 }
 
 // two_line_segment_intersection_parameters (geometry.py:370-445) followed by
 // two_line_segments_intersect (geometry.py:448-475, half-open 0 <= t,u < 1).
+// True only when the rounded quotient fl(n / d) is certainly outside [0, 1),
+// decided on the bits without dividing (integer operations; GB300 runs FP64
+// at 2 lanes per clock per SM and a division is about ten FP64 operations).
+// For |d| < 2^52 (finite):
+//   d == 0                  -> n / d is +-inf or NaN;
+//   |n| >= |d|              -> |n / d| >= 1, rounds to a magnitude >= 1;
+//   n, d of opposite signs  -> n / d < 0, and with |n| >= 2^-1022 its
+//                              magnitude exceeds 2^-1075, so it rounds to a
+//                              negative number, not to -0.
+// Anything else returns false and the caller divides, so the test it
+// guards gives the same answer as dividing every time.
+__device__ __forceinline__ bool quotient_outside_unit(double n, double d) {
+    const unsigned long long abs_mask = 0x7fffffffffffffffull;
+    const unsigned long long nb = (unsigned long long)__double_as_longlong(n);
+    const unsigned long long db = (unsigned long long)__double_as_longlong(d);
+    const unsigned long long na = nb & abs_mask, da = db & abs_mask;
+    if (da >= 0x4330000000000000ull) return false;  // |d| >= 2^52, inf or NaN: divide
+    if (da == 0 || na >= da) return true;
+    return na >= 0x0010000000000000ull && ((nb ^ db) >> 63);
+}
+
+// Where the rounded quotient fl(n / d) lies against [0, 1), decided on the
+// bits when that is certain: 0 outside, 1 inside, -1 undecided (divide).
+// Inside is certain for n == 0, or n and d of one sign with |n| at least two
+// representable steps below |d|: then n / d <= 1 - 2^-52, which rounds
+// below 1.  Outside follows quotient_outside_unit.  A NaN n is undecided.
+__device__ __forceinline__ int quotient_in_unit(double n, double d) {
+    const unsigned long long abs_mask = 0x7fffffffffffffffull;
+    const unsigned long long nb = (unsigned long long)__double_as_longlong(n);
+    const unsigned long long db = (unsigned long long)__double_as_longlong(d);
+    const unsigned long long na = nb & abs_mask, da = db & abs_mask;
+    if (da >= 0x4330000000000000ull || na > 0x7ff0000000000000ull) return -1;
+    if (da == 0 || na >= da) return 0;
+    if (na == 0) return 1;
+    if ((nb ^ db) >> 63) return na >= 0x0010000000000000ull ? 0 : -1;
+    return na + 2 <= da ? 1 : -1;
+}
+
 __device__ __forceinline__ bool seg_hit(double x1, double y1, double x2, double y2, double x3,
                                         double y3, double x4, double y4, double* t_out) {
     if (!bboxes_intersect(x1, y1, x2, y2, x3, y3, x4, y4)) return false;
     double tdet = dsub(dmul(dsub(x1, x3), dsub(y3, y4)), dmul(dsub(y1, y3), dsub(x3, x4)));
     double udet = dsub(dmul(dsub(x1, x2), dsub(y1, y3)), dmul(dsub(y1, y2), dsub(x1, x3)));
     double det = dsub(dmul(dsub(x1, x2), dsub(y3, y4)), dmul(dsub(y1, y2), dsub(x3, x4)));
+    // most candidate edges miss: reject them before the two divisions
+    if (quotient_outside_unit(tdet, det) || quotient_outside_unit(-udet, det)) return false;
     double t = ddiv(tdet, det);
     double u = ddiv(-udet, det);
     *t_out = t;
@@ -626,8 +683,14 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
         } else {
             // _step_inside_static: first crossed edge of the current static
             // cell other than the entry edge
+            // The hit test of each candidate edge is seg_hit's, with the two
+            // quotients placed against [0, 1) on their bits where that is
+            // certain (almost always); only the edge found needs its crossing
+            // parameter divided out.  Same edges, same order, same t.
             const double p2x = x2, p2y = y2;
+            const double dx12 = dsub(x1, p2x), dy12 = dsub(y1, p2y);
             int found = -1;
+            double f_tdet = 0.0, f_det = 1.0;
 #pragma unroll 1
             for (int v = 0; v < 4; v++) {
                 if (v == edge_last) continue;
@@ -636,13 +699,28 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
                 double y3 = st.Y(stx + c_vtx_i[vp], sty + c_vtx_j[vp]);
                 double x4 = st.X(stx + c_vtx_i[v], sty + c_vtx_j[v]);
                 double y4 = st.Y(stx + c_vtx_i[v], sty + c_vtx_j[v]);
-                double t;
-                if (seg_hit(x1, y1, p2x, p2y, x3, y3, x4, y4, &t)) {
-                    x2 = dadd(x1, dmul(t, dsub(p2x, x1)));
-                    y2 = dadd(y1, dmul(t, dsub(p2y, y1)));
-                    found = v;
-                    break;
+                if (!bboxes_intersect(x1, y1, p2x, p2y, x3, y3, x4, y4)) continue;
+                const double x13 = dsub(x1, x3), y13 = dsub(y1, y3);
+                const double x34 = dsub(x3, x4), y34 = dsub(y3, y4);
+                const double tdet = dsub(dmul(x13, y34), dmul(y13, x34));
+                const double udet = dsub(dmul(dx12, y13), dmul(dy12, x13));
+                const double det = dsub(dmul(dx12, y34), dmul(dy12, x34));
+                const int in_t = quotient_in_unit(tdet, det);
+                const int in_u = quotient_in_unit(-udet, det);
+                if (in_t == 0 || in_u == 0) continue;
+                if (in_t < 0 || in_u < 0) {
+                    const double t = ddiv(tdet, det), u = ddiv(-udet, det);
+                    if (!((0 <= t && t < 1) && (0 <= u && u < 1))) continue;
                 }
+                found = v;
+                f_tdet = tdet;
+                f_det = det;
+                break;
+            }
+            if (found >= 0) {
+                const double t = ddiv(f_tdet, f_det);
+                x2 = dadd(x1, dmul(t, dsub(p2x, x1)));
+                y2 = dadd(y1, dmul(t, dsub(p2y, y1)));
             }
             int64_t nsy, nstx, nsty;
             if (found >= 0) {
@@ -659,6 +737,11 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
             // _calc_and_save_weights: area_triangle, negated for axis 0
             double area = dmul(dsub(dmul(x1, y2), dmul(x2, y1)), 0.5);
             if (F.axis == 0) area = -area;
+            // when the static grid is the input grid both sides share the
+            // input cell, and -area / a_in (times w_in) is exactly the
+            // negation of area / a_in (times w_in): one division serves both
+            double w_static = 0.0;
+            bool have_static = false;
 #pragma unroll
             for (int side = 0; side < 2; side++) {
                 int64_t is = side == 0 ? li - 1 : li;
@@ -672,9 +755,18 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
                 int64_t in_flat = ii * P.ncy_in + ij;
                 if (WRITE) {
                     if (wpos < wend) {
-                        double ain = __ldg(P.area_in + in_flat);
-                        double w = side == 0 ? ddiv(area, ain) : ddiv(-area, ain);
-                        if (P.w_in) w = dmul(w, __ldg(P.w_in + in_flat));
+                        double w;
+                        if (!F.sweep_input && have_static) {
+                            w = -w_static;
+                        } else {
+                            double ain = __ldg(P.area_in + in_flat);
+                            w = side == 0 ? ddiv(area, ain) : ddiv(-area, ain);
+                            if (P.w_in) w = dmul(w, __ldg(P.w_in + in_flat));
+                            if (!F.sweep_input && side == 0) {
+                                w_static = w;
+                                have_static = true;
+                            }
+                        }
                         raw_in[wpos] = (int32_t)in_flat;
                         raw_out[wpos] = (int32_t)(oi * P.ncy_out + oj);
                         raw_val[wpos] = w;

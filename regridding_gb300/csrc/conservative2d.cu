@@ -557,12 +557,26 @@ __global__ void __launch_bounds__(128) seat_kernel(Batch B, Seat* seats) {
     seat.pad = 0;
     bool in_box = (S.blx <= x1 && x1 <= S.bux) && (S.bly <= y1 && y1 <= S.buy);
     if (in_box) {
+        // Winding number of the boundary polygon at the line's first vertex.
+        // Only edges whose y-range holds y1 have a nonzero term, and all of
+        // them lie in the row of edge bins at y1's bin (bin_coord is
+        // monotone); an edge spanning several x-bins of the row is counted
+        // in its first.  The boundary edges run along the polygon's order on
+        // the faces j = 0 and i = nx - 1 and against it on i = 0 and
+        // j = ny - 1 (codes 0 and 3), where their ends are swapped back.
+        // The terms are 0, +-1/2 and +-1, so the sum is exact in any order.
         double w = 0;
-        for (int64_t v = lane; v < S.nbound; v += 32) {
-            double ax, ay, bx, by;
-            boundary_vertex(S.g, v == 0 ? S.nbound - 1 : v - 1, &ax, &ay);
-            boundary_vertex(S.g, v, &bx, &by);
-            w += winding_term(x1, y1, ax, ay, bx, by);
+        const Bins& BN = S.bins;
+        const int row = bin_coord(y1, BN.oy, BN.inv_h, BN.nby);
+        for (int bx = lane; bx < BN.nbx; bx += 32) {
+            const int64_t bin = (int64_t)row * BN.nbx + bx;
+            const int32_t q0 = __ldg(BN.ptr + bin), q1 = __ldg(BN.ptr + bin + 1);
+            for (int32_t q = q0; q < q1; q++) {
+                const Edge e = S.edges[__ldg(BN.items + q)];
+                if (bin_coord(fmin(e.x3, e.x4), BN.ox, BN.inv_h, BN.nbx) != bx) continue;
+                if (e.code == 0 || e.code == 3) w += winding_term(x1, y1, e.x4, e.y4, e.x3, e.y3);
+                else w += winding_term(x1, y1, e.x3, e.y3, e.x4, e.y4);
+            }
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) w += __shfl_xor_sync(0xffffffffu, w, o);

@@ -6,7 +6,9 @@ computation is a call into ``libregrid_gb300.so``.
 
 from __future__ import annotations
 
+import concurrent.futures
 import ctypes
+import os
 import threading
 import warnings
 import weakref
@@ -59,8 +61,52 @@ def empty(shape, dtype):
     return t.empty(shape, dtype=dtype, device="cuda")
 
 
+# Large results go into a new host array whose pages are first touched by
+# several threads: on the Grace host a device-to-host copy into untouched
+# pageable memory runs at 14-25 GB/s (the copy takes every page fault on one
+# thread), 16 threads touch 1.4 GB in ~6 ms, and the copy into touched
+# memory then runs at ~190 GB/s.  Page-locked buffers would need a 80-150 ms
+# allocation per 1.4 GB whenever the caller keeps the previous result.
+PARALLEL_TOUCH_BYTES = 16 << 20
+TOUCH_THREADS = min(16, os.cpu_count() or 1)
+_touch_pool = None
+_touch_lock = threading.Lock()
+
+
+def _touch_pool_get():
+    global _touch_pool
+    with _touch_lock:
+        if _touch_pool is None:
+            _touch_pool = concurrent.futures.ThreadPoolExecutor(max_workers=TOUCH_THREADS,
+                                                                thread_name_prefix="regrid-touch")
+        return _touch_pool
+
+
+def host_empty(shape, dtype) -> np.ndarray:
+    """``numpy.empty`` with every page already faulted in (in parallel)."""
+    a = np.empty(shape, dtype=dtype)
+    if a.nbytes < PARALLEL_TOUCH_BYTES:
+        return a
+    b = a.reshape(-1).view(np.uint8)
+    page = os.sysconf("SC_PAGE_SIZE") if hasattr(os, "sysconf") else 4096
+    pool = _touch_pool_get()
+    parts = TOUCH_THREADS
+    edges = np.linspace(0, b.size // page, parts + 1).astype(np.int64) * page
+
+    def touch(k):
+        b[edges[k]:edges[k + 1]:page] = 0
+
+    list(pool.map(touch, range(parts)))
+    return a
+
+
 def download(t) -> np.ndarray:
-    return t.detach().cpu().numpy()
+    t = t.detach()
+    if t.is_cuda and t.numel() * t.element_size() >= PARALLEL_TOUCH_BYTES:
+        a = host_empty(tuple(t.shape), np.dtype(str(t.dtype).replace("torch.", "")))
+        torch().from_numpy(a).copy_(t)
+        return a
+    return t.cpu().numpy()
 
 
 _TORCH_DTYPES = {}

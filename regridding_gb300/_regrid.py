@@ -74,7 +74,8 @@ def regrid_from_weights(
     if values_output is None:
         if accumulate == "fast" and values_input.dtype == np.float32:
             out_dtype = np.float32
-        values_output = np.zeros(full_out, dtype=out_dtype)
+        # every element is written below; pages pre-faulted for the copy-back
+        values_output = _device.host_empty(full_out, out_dtype)
     else:
         if values_output.shape != full_out:
             raise ValueError(f"{values_output.shape=} should be equal to {full_out}")
@@ -111,7 +112,12 @@ def regrid_from_weights(
             first[key] = d
         groups[key].append(d)
 
-    result = np.empty((flat.size, n_out), dtype=out_np_dtype)
+    # one weights element and a row-major output view: the device result is
+    # copied straight into values_output
+    direct = None
+    if len(groups) == 1 and v_out_view.flags.c_contiguous and v_out_view.dtype == out_np_dtype:
+        direct = v_out_view.reshape(flat.size, n_out)
+    result = None if direct is not None else np.empty((flat.size, n_out), dtype=out_np_dtype)
     d_all = None
     if len(groups) == 1:
         d_all = _device.upload(v_in, in_dtype)
@@ -133,13 +139,15 @@ def regrid_from_weights(
             src = _device.upload(v_in[rows], in_dtype)
         dst = t.empty((len(rows), n_out), dtype=_device.torch_dtype(out_np_dtype), device="cuda")
         dw.apply(src, out=dst, accumulate=accumulate)
-        if d_all is not None and len(rows) == flat.size:
+        if direct is not None:
+            t.from_numpy(direct).copy_(dst)
+        elif d_all is not None and len(rows) == flat.size:
             result[:] = _device.download(dst)
         else:
             result[rows] = _device.download(dst)
 
-    values_output_r = result.reshape(shape_out_tmp)
-    v_out_view[...] = values_output_r
+    if result is not None:
+        v_out_view[...] = result.reshape(shape_out_tmp)
     values_output = np.moveaxis(v_out_view, numba_out, axis_output)
 
     if unit_weights is not None:

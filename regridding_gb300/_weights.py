@@ -75,6 +75,18 @@ def _weights_device(coordinates_input, coordinates_output, axis_input, axis_outp
     return array, shape_in, shape_out, dev
 
 
+def _elements(nd: int, h_in, h_out, h_val, counts) -> np.ndarray:
+    """The saved layout's elements as read-only views of the first
+    ``counts[d]`` entries of row ``d`` of the downloaded (nd, cap) arrays:
+    no per-element copy (10^5 spectra of ~1,800 entries are 4.3 GB)."""
+    for a in (h_in, h_out, h_val):
+        a.flags.writeable = False
+    flat = np.empty(nd, dtype=object)
+    for d, c in enumerate(counts):
+        flat[d] = (h_in[d, :c], h_out[d, :c], h_val[d, :c])
+    return flat
+
+
 def _freeze(*arrays):
     for a in arrays:
         a.flags.writeable = False
@@ -176,11 +188,7 @@ def _conservative_1d(x_in, x_out, axi, axo, weights_input, shape_orth):
               sw, cap, _device.ptr(ind_in), _device.ptr(ind_out), _device.ptr(val), _device.ptr(count),
               _device.stream())
     h_in, h_out, h_val, h_cnt = (_device.download(a) for a in (ind_in, ind_out, val, count))
-    flat = np.empty(nd, dtype=object)
-    for d in range(nd):
-        c = int(h_cnt[d])
-        flat[d] = _freeze(h_in[d, :c].copy(), h_out[d, :c].copy(), h_val[d, :c].copy())
-    return flat.reshape(shape_orth), [None] * nd
+    return _elements(nd, h_in, h_out, h_val, h_cnt.tolist()).reshape(shape_orth), [None] * nd
 
 
 # ---------------------------------------------------------------------------
@@ -237,7 +245,5 @@ def _multilinear(ci, co, axis_input, axis_output, weights_input, bounds, perturb
         raise ValueError(
             f"{n_out.value} of the output points fall outside the input grid, and {bounds=}.")
     h_in, h_out, h_val = (_device.download(a) for a in (ind_in, ind_out, val))
-    flat = np.empty(nd, dtype=object)
-    for d in range(nd):
-        flat[d] = _freeze(h_in[d].copy(), h_out[d].copy(), h_val[d].copy())
-    return flat.reshape(shape_orth), shape_in, shape_out, [None] * nd
+    return _elements(nd, h_in, h_out, h_val, [h_in.shape[1]] * nd).reshape(shape_orth), shape_in, shape_out, \
+        [None] * nd

@@ -338,6 +338,19 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes);
  * cache by grid hash). */
 int rg_hash64(const void* h_data, int64_t nbytes, uint64_t seed, uint64_t* h_out);
 
+/* Copy nbytes from host memory (pageable or not) to the device on the
+ * stream: on devices whose kernels access pageable host memory (Grace: ATS
+ * over NVLink-C2C) by a kernel that reads the host array, so the copy does
+ * not queue on the copy engines behind other streams' transfers; elsewhere
+ * cudaMemcpyAsync.  Returns once the source has been read. */
+int rg_copy_from_host(void* d_dst, const void* h_src, int64_t nbytes, rg_stream_t stream);
+
+/* Attributes of the current device that choose the host-transfer strategy,
+ * the first n of: SM count, asynchronous copy engines, pageable memory access
+ * from kernels, whether that uses the host page tables, host pointers usable
+ * for registered memory, concurrent managed access.  Host array of int64. */
+int rg_device_attributes(int64_t* h_out, int n);
+
 #ifdef __cplusplus
 }
 #endif

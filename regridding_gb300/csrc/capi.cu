@@ -210,6 +210,86 @@ int ensure_transposed(rg_weights_s* W, cudaStream_t s) {
     return st;
 }
 
+namespace {
+
+__global__ void host_bytes_copy(unsigned char* __restrict__ dst, const unsigned char* __restrict__ src, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if ((((uintptr_t)dst | (uintptr_t)src | n) & 7) == 0) {
+        unsigned long long* d8 = (unsigned long long*)dst;
+        const unsigned long long* s8 = (const unsigned long long*)src;
+        for (size_t k = t0; k < n / 8; k += stride) d8[k] = s8[k];
+    } else {
+        for (size_t k = t0; k < n; k += stride) dst[k] = src[k];
+    }
+}
+
+__global__ void zero_bytes(unsigned char* __restrict__ p, size_t n) {
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t t0 = blockIdx.x * (size_t)blockDim.x + threadIdx.x;
+    if ((((uintptr_t)p | n) & 7) == 0) {
+        unsigned long long* p8 = (unsigned long long*)p;
+        for (size_t k = t0; k < n / 8; k += stride) p8[k] = 0ull;
+    } else {
+        for (size_t k = t0; k < n; k += stride) p[k] = 0;
+    }
+}
+
+int g_host_access = -1;  // -1: not queried yet
+std::mutex g_host_access_mu;
+
+}  // namespace
+
+bool kernel_host_access() {
+    std::lock_guard<std::mutex> lock(g_host_access_mu);
+    if (g_host_access < 0) {
+        int dev = 0, v = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+            cudaGetLastError();
+            v = 0;
+        }
+        g_host_access = v ? 1 : 0;
+    }
+    return g_host_access == 1;
+}
+
+static unsigned small_blocks(size_t n) {
+    const size_t b = (n / 8 + 255) / 256;
+    return (unsigned)(b < 1 ? 1 : (b > 64 ? 64 : b));
+}
+
+int zero_async(void* p, size_t n, cudaStream_t s) {
+    if (n == 0) return RG_OK;
+    const size_t b = (n / 8 + 255) / 256;
+    zero_bytes<<<(unsigned)(b < 1 ? 1 : (b > 1024 ? 1024 : b)), 256, 0, s>>>((unsigned char*)p, n);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+int small_to_host(void* h_dst, const void* d_src, size_t n, cudaStream_t s) {
+    if (n == 0) return RG_OK;
+    if (!kernel_host_access()) {
+        RG_CUDA(cudaMemcpyAsync(h_dst, d_src, n, cudaMemcpyDeviceToHost, s));
+        return RG_OK;
+    }
+    host_bytes_copy<<<small_blocks(n), 256, 0, s>>>((unsigned char*)h_dst, (const unsigned char*)d_src, n);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+int small_to_device(void* d_dst, const void* h_src, size_t n, cudaStream_t s) {
+    if (n == 0) return RG_OK;
+    if (!kernel_host_access()) {
+        RG_CUDA(cudaMemcpyAsync(d_dst, h_src, n, cudaMemcpyHostToDevice, s));
+        return RG_OK;
+    }
+    host_bytes_copy<<<small_blocks(n), 256, 0, s>>>((unsigned char*)d_dst, (const unsigned char*)h_src, n);
+    RG_CUDA(cudaGetLastError());
+    RG_CUDA(cudaStreamSynchronize(s));
+    return RG_OK;
+}
+
 }  // namespace rg
 
 using namespace rg;
@@ -217,6 +297,28 @@ using namespace rg;
 extern "C" {
 
 int rg_version(void) { return 100; }
+
+int rg_copy_from_host(void* d_dst, const void* h_src, int64_t nbytes, rg_stream_t stream) {
+    RG_CHECK(nbytes >= 0 && (nbytes == 0 || (d_dst && h_src)), RG_ERR_ARG, "rg_copy_from_host: bad arguments");
+    return small_to_device(d_dst, h_src, (size_t)nbytes, (cudaStream_t)stream);
+}
+
+int rg_device_attributes(int64_t* h_out, int n) {
+    RG_CHECK(h_out && n >= 0, RG_ERR_ARG, "rg_device_attributes: NULL output");
+    int dev = 0;
+    RG_CUDA(cudaGetDevice(&dev));
+    const cudaDeviceAttr attrs[] = {cudaDevAttrMultiProcessorCount, cudaDevAttrAsyncEngineCount,
+                                    cudaDevAttrPageableMemoryAccess,
+                                    cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                                    cudaDevAttrCanUseHostPointerForRegisteredMem, cudaDevAttrConcurrentManagedAccess};
+    const int na = (int)(sizeof(attrs) / sizeof(attrs[0]));
+    for (int k = 0; k < n && k < na; ++k) {
+        int v = 0;
+        RG_CUDA(cudaDeviceGetAttribute(&v, attrs[k], dev));
+        h_out[k] = v;
+    }
+    return RG_OK;
+}
 
 int rg_last_error(char* buf, size_t n) {
     size_t len = strlen(g_err);

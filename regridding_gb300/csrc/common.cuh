@@ -117,6 +117,21 @@ struct FastDiv {
     }
 };
 
+// Small host <-> device transfers (sizes, flags, per-pair parameters).  On a
+// device whose kernels read and write pageable host memory (the Grace host
+// of a GB300: address translation over NVLink-C2C) a small kernel moves
+// them, so they do not queue on the copy engines behind other streams' large
+// transfers (a 512^2 build took 6-9 ms instead of 1.3 ms next to a stream
+// copying 600 MB blocks); elsewhere cudaMemcpyAsync.  small_to_host is
+// stream-ordered: read the destination after synchronising the stream.
+// small_to_device returns once the source has been read (it synchronises the
+// stream when a kernel did the copy), so the source may be freed at once.
+bool kernel_host_access();
+// cudaMemsetAsync(p, 0, n, s) as a kernel, for the small clears of the build
+int zero_async(void* p, size_t n, cudaStream_t s);
+int small_to_host(void* h_dst, const void* d_src, size_t n, cudaStream_t s);
+int small_to_device(void* d_dst, const void* h_src, size_t n, cudaStream_t s);
+
 inline unsigned grid_for(int64_t n, int block) {
     int64_t g = (n + block - 1) / block;
     if (g < 1) g = 1;

@@ -1186,14 +1186,14 @@ int prepare_static_count(const double* x, const double* y, int64_t nx, int64_t n
     RG_TRY(dalloc(&R->counts, (size_t)nbins + 1, s));
     RG_TRY(dalloc(&R->ptr64, (size_t)nbins + 1, s));
     RG_TRY(dalloc(&R->ptr32, (size_t)nbins + 1, s));
-    RG_CUDA(cudaMemsetAsync(R->counts, 0, sizeof(unsigned) * (nbins + 1), s));
+    RG_TRY(zero_async(R->counts, sizeof(unsigned) * (nbins + 1), s));
     bin_edges_kernel<false><<<grid_for(nedges, 128), 128, 0, s>>>(R->edges, nedges, b, R->counts, nullptr, nullptr);
     return exclusive_scan_u32_to_i64(R->counts, R->ptr64, nbins + 1, total_dev, s);
 }
 
 int prepare_static_fill(Static* S, StaticPrep* R, int64_t total, cudaStream_t s) {
     RG_TRY(dalloc(&R->items, (size_t)total, s));
-    RG_CUDA(cudaMemsetAsync(R->counts, 0, sizeof(unsigned) * (R->nbins + 1), s));
+    RG_TRY(zero_async(R->counts, sizeof(unsigned) * (R->nbins + 1), s));
     bin_edges_kernel<true><<<grid_for(R->nedges, 128), 128, 0, s>>>(R->edges, R->nedges, S->bins, R->counts,
                                                                      R->items, R->ptr64);
     i64_to_i32<<<grid_for(R->nbins + 1, 256), 256, 0, s>>>(R->ptr64, R->ptr32, R->nbins + 1);
@@ -1279,7 +1279,7 @@ int walk_status(unsigned fl) {
 template <typename T>
 int upload(T** d, const std::vector<T>& h, cudaStream_t s) {
     RG_TRY(dalloc(d, h.size(), s));
-    RG_CUDA(cudaMemcpyAsync(*d, h.data(), sizeof(T) * h.size(), cudaMemcpyHostToDevice, s));
+    RG_TRY(small_to_device(*d, h.data(), sizeof(T) * h.size(), s));
     return RG_OK;
 }
 
@@ -1293,11 +1293,11 @@ int sweep_lines(const Batch& B, int64_t lines, const Seat* seats, int64_t* total
         if ((st = dalloc(&counts, (size_t)lines + 1, s))) break;
         if ((st = dalloc(&offsets, (size_t)lines + 1, s))) break;
         walk_kernel<false><<<grid_for(lines, 64), 64, 0, s>>>(B, seats, counts, nullptr, nullptr, nullptr, nullptr);
-        cudaMemsetAsync(counts + lines, 0, sizeof(int64_t), s);
+        zero_async(counts + lines, sizeof(int64_t), s);
         if ((st = exclusive_scan_i64(counts, offsets, lines + 1, total_dev, s))) break;
         int64_t nraw = 0;
-        cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(fl.data(), B.flags, sizeof(unsigned) * fl.size(), cudaMemcpyDeviceToHost, s);
+        small_to_host(&nraw, total_dev, sizeof(int64_t), s);
+        small_to_host(fl.data(), B.flags, sizeof(unsigned) * fl.size(), s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative sweep (count walk): %s", cudaGetErrorString(e));
@@ -1397,15 +1397,15 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
         if ((st = dalloc(&s_in, (size_t)slots, s))) break;
         if ((st = dalloc(&s_out, (size_t)slots, s))) break;
         if ((st = dalloc(&s_val, (size_t)slots, s))) break;
-        cudaMemsetAsync(n_rep, 0, sizeof(unsigned long long), s);
+        zero_async(n_rep, sizeof(unsigned long long), s);
         chunk_seat_kernel<<<grid_for(chunks, 128), 128, 0, s>>>(B, seats, starts);
         chunk_walk_kernel<<<grid_for(chunks, 64), 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val);
         chunk_repair_kernel<<<grid_for(lines, 64), 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val, n_rep);
-        cudaMemsetAsync(counts + chunks, 0, sizeof(int64_t), s);
+        zero_async(counts + chunks, sizeof(int64_t), s);
         if ((st = exclusive_scan_i64(counts, offsets, chunks + 1, total_dev, s))) break;
         int64_t nraw = 0;
-        cudaMemcpyAsync(&nraw, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(fl.data(), B.flags, sizeof(unsigned) * fl.size(), cudaMemcpyDeviceToHost, s);
+        small_to_host(&nraw, total_dev, sizeof(int64_t), s);
+        small_to_host(fl.data(), B.flags, sizeof(unsigned) * fl.size(), s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative sweep (chunked walk): %s", cudaGetErrorString(e));
@@ -1416,7 +1416,7 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
         for (unsigned f : fl) cap = cap || (f & FLAG_CAPACITY);
         if (cap) {
             overflow = true;
-            cudaMemsetAsync(B.flags, 0, sizeof(unsigned) * fl.size(), s);
+            zero_async(B.flags, sizeof(unsigned) * fl.size(), s);
             break;
         }
         if (nraw >= (int64_t)UINT32_MAX) {
@@ -1545,7 +1545,7 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         }
         if (st) break;
         std::vector<double> bbox_h((size_t)8 * G);
-        cudaMemcpyAsync(bbox_h.data(), bbox_d, sizeof(double) * 8 * G, cudaMemcpyDeviceToHost, s);
+        small_to_host(bbox_h.data(), bbox_d, sizeof(double) * 8 * G, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative build: %s", cudaGetErrorString(e));
@@ -1567,7 +1567,7 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         }
         if (st) break;
         std::vector<int64_t> totals_h((size_t)2 * G);
-        cudaMemcpyAsync(totals_h.data(), totals, sizeof(int64_t) * 2 * G, cudaMemcpyDeviceToHost, s);
+        small_to_host(totals_h.data(), totals, sizeof(int64_t) * 2 * G, s);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative build: %s", cudaGetErrorString(e));
@@ -1608,7 +1608,7 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         if ((st = upload(&out_base_dev, out_base, s))) break;
         if ((st = dalloc(&flags, (size_t)G, s))) break;
         if ((st = dalloc(&total_dev, 1, s))) break;
-        cudaMemsetAsync(flags, 0, sizeof(unsigned) * G, s);
+        zero_async(flags, sizeof(unsigned) * G, s);
         Batch B;
         B.P = P_dev;
         B.C = nullptr;
@@ -1645,7 +1645,7 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         if ((st = dalloc(&tmp_col, (size_t)nraw, s))) break;
         if ((st = dalloc(&tmp_val, (size_t)nraw, s))) break;
         if ((st = dalloc(&row_nnz, (size_t)n_out_all + 1, s))) break;
-        cudaMemsetAsync(row_nnz + n_out_all, 0, sizeof(int64_t), s);
+        zero_async(row_nnz + n_out_all, sizeof(int64_t), s);
         merge_rows<<<grid_for(n_out_all, 128), 128, 0, s>>>(bucket_ptr, perm, raw_in, raw_val, n_out_all, tmp_col,
                                                             tmp_val, row_nnz);
         if ((st = dalloc(&row_ptr, (size_t)n_out_all + 1, s))) break;
@@ -1653,9 +1653,9 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         if ((st = dalloc(&nnz_base_dev, (size_t)G + 1, s))) break;
         nnz_bases<<<grid_for(G + 1, 128), 128, 0, s>>>(row_ptr, out_base_dev, G, nnz_base_dev);
         std::vector<int64_t> nnz_base((size_t)G + 1, 0);
-        cudaMemcpyAsync(nnz_base.data(), nnz_base_dev, sizeof(int64_t) * (G + 1), cudaMemcpyDeviceToHost, s);
+        small_to_host(nnz_base.data(), nnz_base_dev, sizeof(int64_t) * (G + 1), s);
         std::vector<unsigned> fl2((size_t)G, 0u);
-        cudaMemcpyAsync(fl2.data(), flags, sizeof(unsigned) * G, cudaMemcpyDeviceToHost, s);
+        small_to_host(fl2.data(), flags, sizeof(unsigned) * G, s);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative build (merge): %s", cudaGetErrorString(e));

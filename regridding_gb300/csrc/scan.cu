@@ -79,7 +79,7 @@ __global__ void __launch_bounds__(SCAN_BLOCK)
 template <typename T>
 int scan_impl(const T* in, int64_t* out, int64_t n, int64_t* total_dev, cudaStream_t s) {
     if (n <= 0) {
-        if (total_dev) RG_CUDA(cudaMemsetAsync(total_dev, 0, sizeof(int64_t), s));
+        if (total_dev) RG_TRY(zero_async(total_dev, sizeof(int64_t), s));
         return RG_OK;
     }
     int64_t tiles = (n + SCAN_TILE - 1) / SCAN_TILE;

@@ -111,12 +111,12 @@ int bucket_sort(const int32_t* bucket, const int64_t* skey, int64_t n, int64_t n
         if ((st = dalloc(&tmp_idx, (size_t)n, s))) break;
         if ((st = dalloc(&tmp_key, (size_t)n, s))) break;
         if ((st = dalloc(&long_list, (size_t)nbuckets, s))) break;
-        cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbuckets + 1), s);
-        cudaMemsetAsync(long_count, 0, sizeof(unsigned), s);
+        zero_async(counts, sizeof(unsigned) * (nbuckets + 1), s);
+        zero_async(long_count, sizeof(unsigned), s);
         if (n > 0) count_buckets<<<grid_for(n, 256) > 4096 ? 4096 : grid_for(n, 256), 256, 0, s>>>(
             bucket, n, counts);
         if ((st = exclusive_scan_u32_to_i64(counts, bucket_ptr, nbuckets + 1, nullptr, s))) break;
-        cudaMemsetAsync(counts, 0, sizeof(unsigned) * (nbuckets + 1), s);
+        zero_async(counts, sizeof(unsigned) * (nbuckets + 1), s);
         if (n > 0) {
             unsigned g = grid_for(n, 256) > 8192 ? 8192 : grid_for(n, 256);
             scatter_buckets<<<g, 256, 0, s>>>(bucket, skey, n, bucket_ptr, counts, tmp_idx, tmp_key);

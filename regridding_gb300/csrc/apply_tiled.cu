@@ -941,8 +941,8 @@ int prepare_tiled(rg_weights_s* W, int grain, cudaStream_t s) {
         if ((st = exclusive_scan_i64(glen, W->t_gptr[g], tiles + 1, total_dev, s))) break;
         int64_t total = 0;
         unsigned long long hmax = 0;
-        cudaMemcpyAsync(&hmax, maxlen, sizeof(hmax), cudaMemcpyDeviceToHost, s);
-        cudaMemcpyAsync(&total, total_dev, sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+        small_to_host(&hmax, maxlen, sizeof(hmax), s);
+        small_to_host(&total, total_dev, sizeof(int64_t), s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("prepare_tiled: %s", cudaGetErrorString(e));
@@ -1072,7 +1072,7 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         prepare_patch<0><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, W->in_shape1, W->box_origin,
                                                            extent, stats, 0, nullptr);
         unsigned h[4] = {0, 0, 0, 0};
-        cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, s);
+        small_to_host(h, stats, sizeof(h), s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("apply (patch lists): %s", cudaGetErrorString(e));
@@ -1083,7 +1083,7 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         const int BR = (int)((std::min<unsigned>(std::max<unsigned>(h[0], 1u), PBOX_MAX_R) + 3) & ~3u);
         prepare_patch<1><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, W->in_shape1, W->box_origin,
                                                            extent, stats, BR, W->box_slot);
-        cudaMemcpyAsync(h, stats, sizeof(h), cudaMemcpyDeviceToHost, s);
+        small_to_host(h, stats, sizeof(h), s);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("apply (patch lists): %s", cudaGetErrorString(e));
@@ -1308,7 +1308,7 @@ int rows_usable(rg_weights_s* W, const float* vin, int64_t stack, cudaStream_t s
         max_row_len<<<grid_for(W->n_out, 256) > 1024 ? 1024 : grid_for(W->n_out, 256), 256, 0, s>>>(W->row_ptr,
                                                                                                    W->n_out, d);
         unsigned h = 0;
-        cudaMemcpyAsync(&h, d, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        small_to_host(&h, d, sizeof(unsigned), s);
         cudaError_t e = cudaStreamSynchronize(s);
         dfree(d, s);
         if (e != cudaSuccess) {

@@ -427,7 +427,7 @@ int rg_weights_from_coo(const int64_t* d_in, const int64_t* d_out, const double*
         }
         if (nnz > 0) gather_csr<<<capped(nnz, 256), 256, 0, s>>>(perm, in32, d_val, nnz, W->col, W->val);
         unsigned hbad = 0;
-        cudaMemcpyAsync(&hbad, bad, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
+        small_to_host(&hbad, bad, sizeof(unsigned), s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("rg_weights_from_coo: %s", cudaGetErrorString(e));

@@ -362,18 +362,6 @@ __global__ void bbox_combine(const double* __restrict__ part, int nparts, double
     }
 }
 
-// Boundary polygon of grid_boundary (_grids.py:167-215), vertex k.
-__device__ __forceinline__ void boundary_vertex(const Grid& g, int64_t k, double* bx, double* by) {
-    int64_t sx = g.nx, sy = g.ny;
-    int64_t i, j;
-    if (k < sx - 1) { i = k; j = 0; }
-    else if ((k -= sx - 1) < sy - 1) { i = sx - 1; j = k; }
-    else if ((k -= sy - 1) < sx - 1) { i = sx - 1 - k; j = sy - 1; }
-    else { k -= sx - 1; i = 0; j = sy - 1 - k; }
-    *bx = g.X(i, j);
-    *by = g.Y(i, j);
-}
-
 // Boundary edges in the scan order of _step_outside_static (:608-683):
 // axis 0 (faces i = 0 then i = nx-1, running along j), then axis 1 (faces
 // j = 0 then j = ny-1, running along i).

@@ -650,3 +650,26 @@ def test_row_kernel_long_stacks(rg, kind):
     from regridding_gb300 import _lib
 
     _lib.call("rg_weights_check", dw.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+
+
+def test_copy_from_host_and_attributes(torch):
+    """rg_copy_from_host (a kernel reading pageable host memory where the
+    device allows it, else a copy-engine copy) copies every byte, aligned or
+    not; rg_device_attributes reports the SM count."""
+    import ctypes
+
+    from regridding_gb300 import _device, _lib
+
+    attrs = np.zeros(6, np.int64)
+    _lib.call("rg_device_attributes", ctypes.c_void_p(attrs.ctypes.data), 6)
+    assert attrs[0] == torch.cuda.get_device_properties(0).multi_processor_count
+    rng = np.random.default_rng(11)
+    for n in (1, 7, 8, 4096 + 3, 3 << 20):
+        src = rng.integers(0, 256, n + 1, dtype=np.uint8)
+        for off in (0, 1):
+            d = torch.zeros(n, dtype=torch.uint8, device="cuda")
+            _lib.call("rg_copy_from_host", _device.ptr(d), ctypes.c_void_p(src.ctypes.data + off), n,
+                      _device.stream())
+            np.testing.assert_array_equal(d.cpu().numpy(), src[off:off + n])
+    big = rng.normal(0, 1, (1000, 1000))
+    np.testing.assert_array_equal(_device.download(_device.upload(big)), big)

@@ -652,11 +652,13 @@ def test_row_kernel_long_stacks(rg, kind):
     _lib.call("rg_weights_check", dw.handle, ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
 
 
-def test_copy_from_host_and_attributes(torch):
+def test_copy_from_host_and_attributes(rg):
     """rg_copy_from_host (a kernel reading pageable host memory where the
     device allows it, else a copy-engine copy) copies every byte, aligned or
     not; rg_device_attributes reports the SM count."""
     import ctypes
+
+    import torch
 
     from regridding_gb300 import _device, _lib
 

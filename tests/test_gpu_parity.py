@@ -675,3 +675,43 @@ def test_copy_from_host_and_attributes(rg):
             np.testing.assert_array_equal(d.cpu().numpy(), src[off:off + n])
     big = rng.normal(0, 1, (1000, 1000))
     np.testing.assert_array_equal(_device.download(_device.upload(big)), big)
+
+
+BOX_CONFIGS = ["4,2,0,0", "4,2,4,0", "4,3,4,0", "2,3,4,0", "2,4,4,0", "8,2,0,0", "4,3,0,0", "4,2,0,1", "4,3,0,1",
+               "8,2,0,1"]
+
+
+@pytest.mark.parametrize("stack", [1, 7, 64])
+def test_box_configs_agree(rg, stack, monkeypatch):
+    """Every configuration of the tensor-copy apply (slices per stage,
+    stages, register cap; one patch per block or persistent blocks that keep
+    the stage ring filled across patches), forced in turn, gives the same
+    float32 result bit for bit (each output's FMA chain is the same), with
+    some patches on the direct path, and matches the oracle's bound."""
+    import torch
+
+    from regridding_gb300 import _lib
+    from regridding_gb300._device import DeviceWeights
+
+    rng = np.random.default_rng([99, stack])
+    n0_in, n1_in, n0_out, n1_out = 64, 96, 48, 60
+    ii, oo, vv = _local_coo(rng, n0_in, n1_in, n0_out, n1_out)
+    n_in, n_out = n0_in * n1_in, n0_out * n1_out
+    key = np.unique(np.concatenate([oo * n_in + ii, np.array([7, 900]) * n_in + [n_in - 5, 11]]))
+    oo, ii = key // n_in, key % n_in
+    vv = rng.uniform(0.1, 1.0, ii.size)
+    vals = rng.uniform(0.5, 2.0, (stack, n_in)).astype(np.float32)
+    d_vals = torch.from_numpy(vals).cuda()
+    results = []
+    for cfg in BOX_CONFIGS:
+        monkeypatch.setenv("RG_APPLY_BOX_CONFIG", cfg)
+        dw = DeviceWeights.from_coo(ii, oo, vv, n_in, n_out, (n0_out, n1_out))
+        _lib.call("rg_weights_set_input_shape", dw.handle, n0_in, n1_in)
+        results.append(dw.apply(d_vals, accumulate="fast").cpu().numpy())
+        dw.free()
+    for cfg, got in zip(BOX_CONFIGS[1:], results[1:]):
+        np.testing.assert_array_equal(got, results[0], err_msg=cfg)
+    exp = oracle.apply(ii, oo, vv, vals.astype(np.float64), n_out)
+    k = np.bincount(oo, minlength=n_out)
+    bound = (k + 2) * 2.0**-24 * oracle.apply(ii, oo, np.abs(vv), np.abs(vals).astype(np.float64), n_out)
+    assert np.all(np.abs(results[0] - exp) <= bound)

@@ -677,138 +677,6 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     }
 }
 
-// Persistent variant of the fast (float32) path: a block walks the work
-// items (patch, stack chunk) w = blockIdx.x, blockIdx.x + gridDim.x, ...,
-// and thread 0 keeps the stage ring filled across item boundaries, so the
-// boxes of a block's next patch are in flight while it reduces the last
-// groups of the current one (the one-patch-per-block kernel pays a box
-// round trip and its entry loads at every block start).  Ring phases count
-// the block's groups over all its items.  Items whose footprint exceeds the
-// box take the direct path and never touch the ring.
-template <int SPS, int NST>
-__global__ void __launch_bounds__(32 * PATCH_WARPS)
-    apply_patch_tma_p(const __grid_constant__ CUtensorMap tmap, const int64_t* __restrict__ row_ptr,
-                      const int32_t* __restrict__ col, const uint16_t* __restrict__ slot,
-                      const float* __restrict__ bval, const float* __restrict__ val, PatchGrid P,
-                      int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
-                      unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
-                      int64_t n_out, int64_t stack, int64_t chunk, int64_t n_items, unsigned* __restrict__ flags) {
-    __shared__ __align__(8) uint64_t full[NST], empty[NST];
-    extern __shared__ __align__(1024) float ring[];
-    const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
-    const int plane = BR * PBOX_C;
-    const int flip = (BR & 4) ? 16 : 0;
-    if (t == 0) {
-        for (int k = 0; k < NST; k++) {
-            mbar_init(&full[k], 1);
-            mbar_init(&empty[k], PATCH_WARPS);
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
-    __syncthreads();
-
-    // producer cursor (used by thread 0 only): the next (item, group) to load
-    int64_t pw = blockIdx.x, pg = 0, issued = 0;
-    auto next_load = [&]() -> bool {  // moves the cursor to the next load; false when none is left
-        while (pw < n_items) {
-            const int64_t patch = pw % n_patches, ch = pw / n_patches;
-            const int64_t d0 = ch * chunk, d1 = d0 + chunk < stack ? d0 + chunk : stack;
-            if (origin[patch].x >= 0 && pg < (d1 - d0 + SPS - 1) / SPS) return true;
-            pw += gridDim.x;
-            pg = 0;
-        }
-        return false;
-    };
-    auto issue_next = [&]() {  // the cursor's load into stage issued % NST
-        const int64_t patch = pw % n_patches, ch = pw / n_patches;
-        const int2 org = origin[patch];
-        const int st = (int)(issued % NST);
-        mbar_expect_tx(&full[st], stage_bytes);
-        tma_load_3d(ring + (int64_t)st * stage_floats, &tmap, org.y, org.x, (int)(ch * chunk + pg * SPS), &full[st]);
-        pg++;
-        issued++;
-    };
-    auto drain = [&](int64_t consumed) {  // bounded wait for the loads still in flight
-        for (int64_t q = consumed; q < issued; q++) (void)mbar_wait_bounded(&full[q % NST], (unsigned)((q / NST) & 1));
-    };
-    if (t == 0)
-        for (int k = 0; k < NST && next_load(); k++) issue_next();
-
-    int64_t G = 0;  // groups consumed by this block
-    for (int64_t wi = blockIdx.x; wi < n_items; wi += gridDim.x) {
-        const int64_t p = wi % n_patches, ch = wi / n_patches;
-        const int64_t d0 = ch * chunk, d1 = d0 + chunk < stack ? d0 + chunk : stack;
-        const int64_t o = patch_cell(P, p, 4 * (warp >> 1) + (lane >> 3), 8 * (warp & 1) + (lane & 7));
-        int64_t s = 0, e = 0;
-        if (o >= 0) {
-            s = row_ptr[o];
-            e = row_ptr[o + 1];
-        }
-        const int nk = (int)(e - s);
-        float* out = vout + (o >= 0 ? o : 0);
-        const int2 org = origin[p];
-        if (org.x < 0) {
-            if (o >= 0) apply_direct(s, e, col, val, vin, n_in, out, n_out, d0, d1);
-            continue;
-        }
-        int li[CACHED_T];
-        float w[CACHED_T];
-#pragma unroll
-        for (int k = 0; k < CACHED_T; k++) {
-            li[k] = k < nk ? (int)slot[s + k] : 0;
-            w[k] = k < nk ? bval[s + k] : 0.f;
-        }
-        const int64_t ngroups = (d1 - d0 + SPS - 1) / SPS;
-        for (int64_t grp = 0; grp < ngroups; grp++, G++) {
-            const int st = (int)(G % NST);
-            const unsigned ph = (unsigned)((G / NST) & 1);
-            const bool got = mbar_wait_bounded(&full[st], ph);
-            if (!__all_sync(0xffffffffu, got)) {
-                if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
-                if (t == 0) drain(G + 1);
-                return;
-            }
-            const float* buf = ring + (int64_t)st * stage_floats;
-            const int64_t ds = d0 + grp * SPS;
-            if (o >= 0) {
-                float acc[SPS];
-#pragma unroll
-                for (int q = 0; q < SPS; q++) acc[q] = 0.f;
-#pragma unroll
-                for (int k = 0; k < CACHED_T; k++) {
-                    if (k < nk) {
-#pragma unroll
-                        for (int q = 0; q < SPS; q++)
-                            acc[q] = fmaf(w[k], buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))], acc[q]);
-                    }
-                }
-                for (int64_t k = s + CACHED_T; k < e; k++) {
-                    const float wk = bval[k];
-                    const int sk = slot[k];
-#pragma unroll
-                    for (int q = 0; q < SPS; q++)
-                        acc[q] = fmaf(wk, buf[q * plane + (sk ^ ((q & 1) ? flip : 0))], acc[q]);
-                }
-#pragma unroll
-                for (int q = 0; q < SPS; q++)
-                    if (ds + q < d1) out[(ds + q) * n_out] = acc[q];
-            }
-            __syncwarp();
-            if (lane == 0) mbar_arrive(&empty[st]);  // this warp is done with the stage
-            if (t == 0 && next_load()) {
-                // the stage's next load is the block's group G + NST
-                if (!mbar_wait_bounded(&empty[st], ph)) {
-                    atomicOr(flags, FLAG_TIMEOUT);
-                    drain(G + 1);
-                    return;
-                }
-                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-                issue_next();
-            }
-        }
-    }
-}
-
 // ---------------------------------------------------------------------------
 // Row variant, for weights with a short input axis (a whole slice fits in
 // shared memory: 1D multilinear or conservative weights over many spectra).
@@ -1250,10 +1118,9 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
 // times each on the first apply of a handle; RG_APPLY_BOX_CONFIG="sps,nst,minb"
 // forces one.
 struct BoxConfig {
-    int sps, nst, minb, persistent;
+    int sps, nst, minb;
 };
-constexpr BoxConfig kBoxConfigs[] = {{4, 2, 0, 0}, {4, 2, 4, 0}, {4, 3, 4, 0}, {2, 3, 4, 0}, {2, 4, 4, 0},
-                                     {8, 2, 0, 0}, {4, 3, 0, 0}, {4, 2, 0, 1}, {4, 3, 0, 1}, {8, 2, 0, 1}};
+constexpr BoxConfig kBoxConfigs[] = {{4, 2, 0}, {4, 2, 4}, {4, 3, 4}, {2, 3, 4}, {2, 4, 4}, {8, 2, 0}, {4, 3, 0}};
 constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]));
 
 template <int SPS, int NST, int MINB, bool EXACT = false>
@@ -1289,41 +1156,6 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     return RG_OK;
 }
 
-template <int SPS, int NST>
-int launch_patch_persistent(const rg_weights_s* W, const CUtensorMap& map, int box_slices, const float* vin,
-                            float* vout, int64_t stack, cudaStream_t s) {
-    const int BR = W->box_rows;
-    const int stage_floats = (SPS * BR * PBOX_C + 255) & ~255;
-    const unsigned stage_bytes = (unsigned)(box_slices * BR * PBOX_C * 4);
-    const size_t smem = (size_t)NST * stage_floats * sizeof(float);
-    if (smem > 200 * 1024) return RG_ERR_UNSUPPORTED;
-    static std::once_flag attr;
-    std::call_once(attr, []() {
-        cudaFuncSetAttribute(apply_patch_tma_p<SPS, NST>, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
-        cudaGetLastError();
-    });
-    const int64_t patches = W->box_patches;
-    // the stack split as for the one-patch-per-block kernel
-    const int64_t target_blocks = 152 * 4 * 4;
-    int64_t chunks = (target_blocks + patches - 1) / patches;
-    if (chunks < 1) chunks = 1;
-    int64_t chunk = (stack + chunks - 1) / chunks;
-    chunk = (chunk + SPS - 1) / SPS * SPS;
-    const int64_t n_items = patches * ((stack + chunk - 1) / chunk);
-    int dev = 0, sms = 0, per_sm = 0;
-    RG_CUDA(cudaGetDevice(&dev));
-    RG_CUDA(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev));
-    RG_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, apply_patch_tma_p<SPS, NST>, 32 * PATCH_WARPS,
-                                                          smem));
-    if (per_sm < 1) return RG_ERR_UNSUPPORTED;
-    const int64_t blocks = std::min<int64_t>(n_items, (int64_t)sms * per_sm);
-    apply_patch_tma_p<SPS, NST><<<(unsigned)blocks, 32 * PATCH_WARPS, smem, s>>>(
-        map, W->row_ptr, W->col, W->box_slot, W->box_val, W->val32, patch_grid(W), patches, W->box_origin, BR,
-        stage_floats, stage_bytes, vin, W->n_in, vout, W->n_out, stack, chunk, n_items, W->dflags);
-    RG_CUDA(cudaGetLastError());
-    return RG_OK;
-}
-
 // Tensor map of the input stack: columns x rows x slices, boxes of
 // 32 columns x box_rows x bs slices, 128-byte swizzle.
 bool encode_stack(const rg_weights_s* W, const float* vin, int64_t stack, int bs, CUtensorMap* map) {
@@ -1351,9 +1183,6 @@ int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* v
         case 4: return launch_patch<2, 4, 4>(W, map, bs, vin, vout, stack, s);
         case 5: return launch_patch<8, 2, 0>(W, map, bs, vin, vout, stack, s);
         case 6: return launch_patch<4, 3, 0>(W, map, bs, vin, vout, stack, s);
-        case 7: return launch_patch_persistent<4, 2>(W, map, bs, vin, vout, stack, s);
-        case 8: return launch_patch_persistent<4, 3>(W, map, bs, vin, vout, stack, s);
-        case 9: return launch_patch_persistent<8, 2>(W, map, bs, vin, vout, stack, s);
     }
     return RG_ERR_UNSUPPORTED;
 }
@@ -1361,13 +1190,10 @@ int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* v
 int forced_box_config() {
     const char* env = getenv("RG_APPLY_BOX_CONFIG");
     if (!env) return -1;
-    // "sps,nst,minb" or "sps,nst,minb,persistent"
-    int a = 0, b = 0, c = 0, d = 0;
-    if (sscanf(env, "%d,%d,%d,%d", &a, &b, &c, &d) < 3) return -1;
+    int a = 0, b = 0, c = 0;
+    if (sscanf(env, "%d,%d,%d", &a, &b, &c) != 3) return -1;
     for (int k = 0; k < kNumBoxConfigs; k++)
-        if (kBoxConfigs[k].sps == a && kBoxConfigs[k].nst == b && kBoxConfigs[k].minb == c &&
-            kBoxConfigs[k].persistent == d)
-            return k;
+        if (kBoxConfigs[k].sps == a && kBoxConfigs[k].nst == b && kBoxConfigs[k].minb == c) return k;
     return -1;
 }
 

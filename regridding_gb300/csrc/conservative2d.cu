@@ -921,12 +921,10 @@ __device__ __forceinline__ int64_t chunk_end(const ChunkPlan& C, const Family& F
     return e < F.len - 1 ? e : F.len - 1;
 }
 
-__global__ void __launch_bounds__(64)
-    chunk_walk_kernel(Batch B, const WalkState* __restrict__ starts, WalkState* __restrict__ ends,
-                      int64_t* __restrict__ counts, int32_t* __restrict__ s_in, int32_t* __restrict__ s_out,
-                      double* __restrict__ s_val) {
-    int64_t g = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (g >= B.chunk_base[B.G]) return;
+__device__ __forceinline__ void chunk_walk_one(const Batch& B, const WalkState* __restrict__ starts,
+                                               WalkState* __restrict__ ends, int64_t* __restrict__ counts,
+                                               int32_t* __restrict__ s_in, int32_t* __restrict__ s_out,
+                                               double* __restrict__ s_val, int64_t g) {
     const int pg = pair_of(B.chunk_base, B.G, g);
     const SweepParams& P = B.P[pg];
     const ChunkPlan& C = B.C[pg];
@@ -942,6 +940,21 @@ __global__ void __launch_bounds__(64)
     counts[g] = walk_range<true>(P, F, S, li, chunk_end(C, F, c), st, base, base + C.cap[f], s_in, s_out,
                                  s_val, flags, max_steps);
     ends[g] = st;
+}
+
+// Chunks are handed out one at a time from a counter: a thread that finishes
+// a short chunk takes the next one instead of idling until the longest chunk
+// of its warp is done (walk lengths differ between chunks).
+__global__ void __launch_bounds__(64)
+    chunk_walk_kernel(Batch B, const WalkState* __restrict__ starts, WalkState* __restrict__ ends,
+                      int64_t* __restrict__ counts, int32_t* __restrict__ s_in, int32_t* __restrict__ s_out,
+                      double* __restrict__ s_val, unsigned long long* __restrict__ next_chunk) {
+    const int64_t total = B.chunk_base[B.G];
+    for (;;) {
+        const int64_t g = (int64_t)atomicAdd(next_chunk, 1ull);
+        if (g >= total) return;
+        chunk_walk_one(B, starts, ends, counts, s_in, s_out, s_val, g);
+    }
 }
 
 // One thread per line: walk chunks again, in order, wherever a chunk's start
@@ -1381,13 +1394,17 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
         if ((st = dalloc(&ends, (size_t)chunks, s))) break;
         if ((st = dalloc(&counts, (size_t)chunks + 1, s))) break;
         if ((st = dalloc(&offsets, (size_t)chunks + 1, s))) break;
-        if ((st = dalloc(&n_rep, 1, s))) break;
+        if ((st = dalloc(&n_rep, 2, s))) break;  // chunks repaired, next chunk of the walk
         if ((st = dalloc(&s_in, (size_t)slots, s))) break;
         if ((st = dalloc(&s_out, (size_t)slots, s))) break;
         if ((st = dalloc(&s_val, (size_t)slots, s))) break;
-        zero_async(n_rep, sizeof(unsigned long long), s);
+        zero_async(n_rep, 2 * sizeof(unsigned long long), s);
         chunk_seat_kernel<<<grid_for(chunks, 128), 128, 0, s>>>(B, seats, starts);
-        chunk_walk_kernel<<<grid_for(chunks, 64), 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val);
+        {
+            // resident blocks only: 8 blocks of 64 threads per SM
+            const unsigned blocks = std::min<unsigned>(grid_for(chunks, 64), 152u * 8u);
+            chunk_walk_kernel<<<blocks, 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val, n_rep + 1);
+        }
         chunk_repair_kernel<<<grid_for(lines, 64), 64, 0, s>>>(B, starts, ends, counts, s_in, s_out, s_val, n_rep);
         zero_async(counts + chunks, sizeof(int64_t), s);
         if ((st = exclusive_scan_i64(counts, offsets, chunks + 1, total_dev, s))) break;

@@ -149,9 +149,13 @@ int exclusive_scan_u32_to_i64(const unsigned* in, int64_t* out, int64_t n, int64
 // Stable ordering of elements grouped into buckets: given bucket[k] in
 // [0, nbuckets) and a secondary key skey[k] that is unique within each bucket,
 // produce bucket_ptr[nbuckets+1] and perm[n] such that perm lists the
-// elements sorted by (bucket, skey).  Implemented in sort.cu.
+// elements sorted by (bucket, skey).  With a payload (val[k], and out_hi /
+// out_val non-null) the sorted high halves of the keys and the values are
+// written in the same order (out_hi[g] = skey[perm[g]] >> 32, out_val[g] =
+// val[perm[g]]), gathered while ranking.  Implemented in sort.cu.
 int bucket_sort(const int32_t* bucket, const int64_t* skey, int64_t n, int64_t nbuckets,
-                int64_t* bucket_ptr, uint32_t* perm, unsigned* flags, cudaStream_t s);
+                int64_t* bucket_ptr, uint32_t* perm, unsigned* flags, cudaStream_t s,
+                const double* val = nullptr, int32_t* out_hi = nullptr, double* out_val = nullptr);
 
 }  // namespace rg
 

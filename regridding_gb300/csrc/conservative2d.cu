@@ -1088,29 +1088,31 @@ __device__ double pairwise_sum(const At& at, int64_t off, int64_t n) {
     }
 }
 
-struct GatherVal {
-    const double* val;
-    const uint32_t* perm;
-    __device__ __forceinline__ double operator()(int64_t k) const { return val[perm[k]]; }
-};
 
 // One thread per output cell: merge equal input indices of the cell's sorted
 // raw entries with the add.reduceat association, first + pairwise(rest),
 // writing (col, value) compactly from the bucket start; count them.
-__global__ void merge_rows(const int64_t* __restrict__ bptr, const uint32_t* __restrict__ perm,
-                           const int32_t* __restrict__ raw_in, const double* __restrict__ raw_val,
-                           int64_t n_out, int32_t* __restrict__ tmp_col, double* __restrict__ tmp_val,
-                           int64_t* __restrict__ row_nnz) {
-    GatherVal at{raw_val, perm};
+// The sorted raw entries arrive as contiguous (input index, value) arrays
+// (the bucket sort gathers them while ranking), so each thread reads its
+// row's entries in order instead of chasing a permutation.
+struct SortedVal {
+    const double* val;
+    __device__ __forceinline__ double operator()(int64_t k) const { return val[k]; }
+};
+
+__global__ void merge_rows(const int64_t* __restrict__ bptr, const int32_t* __restrict__ s_in,
+                           const double* __restrict__ s_val, int64_t n_out, int32_t* __restrict__ tmp_col,
+                           double* __restrict__ tmp_val, int64_t* __restrict__ row_nnz) {
+    SortedVal at{s_val};
     for (int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; o < n_out;
          o += (int64_t)gridDim.x * blockDim.x) {
         int64_t s = bptr[o], t = bptr[o + 1];
         int64_t w = s;
         int64_t g = s;
         while (g < t) {
-            int32_t c = raw_in[perm[g]];
+            int32_t c = s_in[g];
             int64_t h = g + 1;
-            while (h < t && raw_in[perm[h]] == c) h++;
+            while (h < t && s_in[h] == c) h++;
             double v = dadd(at(g), pairwise_sum(at, g + 1, h - g - 1));
             tmp_col[w] = c;
             tmp_val[w] = v;
@@ -1521,7 +1523,8 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
     Seat* seats = nullptr;
     int64_t* total_dev = nullptr;
     unsigned* flags = nullptr;
-    int32_t *raw_in = nullptr, *raw_out = nullptr;
+    int32_t *raw_in = nullptr, *raw_out = nullptr, *sorted_in = nullptr;
+    double* sorted_val = nullptr;
     double* raw_val = nullptr;
     int64_t* skey = nullptr;
     int64_t* bucket_ptr = nullptr;
@@ -1644,14 +1647,25 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         if ((st = dalloc(&perm, (size_t)nraw, s))) break;
         if (nraw > 0)
             make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(raw_in, nraw, skey);
-        if ((st = bucket_sort(raw_out, skey, nraw, n_out_all, bucket_ptr, perm, flags, s))) break;
+        // the sort also lays the entries' input indices and values out in
+        // sorted order, so the merge reads them contiguously
+        if ((st = dalloc(&sorted_in, (size_t)nraw, s))) break;
+        if ((st = dalloc(&sorted_val, (size_t)nraw, s))) break;
+        if ((st = bucket_sort(raw_out, skey, nraw, n_out_all, bucket_ptr, perm, flags, s, raw_val, sorted_in,
+                              sorted_val)))
+            break;
         dfree(skey, s);
         skey = nullptr;
+        dfree(raw_in, s);
+        dfree(raw_out, s);
+        dfree(raw_val, s);
+        raw_in = raw_out = nullptr;
+        raw_val = nullptr;
         if ((st = dalloc(&tmp_col, (size_t)nraw, s))) break;
         if ((st = dalloc(&tmp_val, (size_t)nraw, s))) break;
         if ((st = dalloc(&row_nnz, (size_t)n_out_all + 1, s))) break;
         zero_async(row_nnz + n_out_all, sizeof(int64_t), s);
-        merge_rows<<<grid_for(n_out_all, 128), 128, 0, s>>>(bucket_ptr, perm, raw_in, raw_val, n_out_all, tmp_col,
+        merge_rows<<<grid_for(n_out_all, 128), 128, 0, s>>>(bucket_ptr, sorted_in, sorted_val, n_out_all, tmp_col,
                                                             tmp_val, row_nnz);
         if ((st = dalloc(&row_ptr, (size_t)n_out_all + 1, s))) break;
         if ((st = exclusive_scan_i64(row_nnz, row_ptr, n_out_all + 1, total_dev, s))) break;
@@ -1772,6 +1786,8 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
     dfree(raw_in, s);
     dfree(raw_out, s);
     dfree(raw_val, s);
+    dfree(sorted_in, s);
+    dfree(sorted_val, s);
     dfree(skey, s);
     dfree(bucket_ptr, s);
     dfree(perm, s);

@@ -11,22 +11,43 @@ namespace {
 constexpr int SMALL_BUCKET = 64;  // ranked by one thread per element
 constexpr int RANK_TILE = 2048;   // keys staged per shared-memory tile for long buckets
 
+// Consecutive elements often share a bucket (a sweep emits the entries of a
+// cell together): the lanes of a warp with the same bucket add to its counter
+// once.  The loops run whole warps (uniform trip counts) for the collectives.
+__device__ __forceinline__ unsigned warp_bucket_add(unsigned* counters, int32_t b, bool active) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned key = active ? (unsigned)b : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const unsigned leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (active && lane == leader) base = atomicAdd(&counters[b], (unsigned)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
 __global__ void count_buckets(const int32_t* bucket, int64_t n, unsigned* counts) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-         k += (int64_t)gridDim.x * blockDim.x)
-        atomicAdd(&counts[bucket[k]], 1u);
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k0 = blockIdx.x * (int64_t)blockDim.x; k0 < n; k0 += stride) {
+        const int64_t k = k0 + threadIdx.x;
+        const bool active = k < n;
+        (void)warp_bucket_add(counts, active ? bucket[k] : 0, active);
+    }
 }
 
 __global__ void scatter_buckets(const int32_t* bucket, const int64_t* skey, int64_t n,
                                 const int64_t* bucket_ptr, unsigned* cursor, uint32_t* tmp_idx,
                                 int64_t* tmp_key) {
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        int32_t b = bucket[k];
-        unsigned pos = atomicAdd(&cursor[b], 1u);
-        int64_t dst = bucket_ptr[b] + pos;
-        tmp_idx[dst] = (uint32_t)k;
-        tmp_key[dst] = skey[k];
+    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+    for (int64_t k0 = blockIdx.x * (int64_t)blockDim.x; k0 < n; k0 += stride) {
+        const int64_t k = k0 + threadIdx.x;
+        const bool active = k < n;
+        const int32_t b = active ? bucket[k] : 0;
+        const unsigned pos = warp_bucket_add(cursor, b, active);
+        if (active) {
+            const int64_t dst = bucket_ptr[b] + pos;
+            tmp_idx[dst] = (uint32_t)k;
+            tmp_key[dst] = skey[k];
+        }
     }
 }
 
@@ -35,7 +56,7 @@ __global__ void scatter_buckets(const int32_t* bucket, const int64_t* skey, int6
 // their buckets listed (once, by the bucket's first element) for rank_long.
 __global__ void rank_small(const int32_t* bucket, const uint32_t* tmp_idx, const int64_t* tmp_key,
                            int64_t n, const int64_t* bucket_ptr, uint32_t* perm, int32_t* long_list,
-                           unsigned* long_count) {
+                           unsigned* long_count, const double* val, int32_t* out_hi, double* out_val) {
     for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < n;
          e += (int64_t)gridDim.x * blockDim.x) {
         uint32_t idx = tmp_idx[e];
@@ -49,13 +70,18 @@ __global__ void rank_small(const int32_t* bucket, const uint32_t* tmp_idx, const
         int64_t rank = 0;
         for (int64_t q = s; q < t; q++) rank += tmp_key[q] < key;
         perm[s + rank] = idx;
+        if (out_val) {
+            out_hi[s + rank] = (int32_t)(key >> 32);
+            out_val[s + rank] = val[idx];
+        }
     }
 }
 
 // One block per long bucket (grid-stride over the list built by rank_small).
 __global__ void __launch_bounds__(256)
     rank_long(const uint32_t* tmp_idx, const int64_t* tmp_key, const int64_t* bucket_ptr,
-              const int32_t* long_list, const unsigned* long_count, uint32_t* perm) {
+              const int32_t* long_list, const unsigned* long_count, uint32_t* perm, const double* val,
+              int32_t* out_hi, double* out_val) {
     __shared__ int64_t tile[RANK_TILE];
     unsigned nl = *long_count;
     for (unsigned li = blockIdx.x; li < nl; li += gridDim.x) {
@@ -86,7 +112,14 @@ __global__ void __launch_bounds__(256)
 #pragma unroll
             for (int r = 0; r < 8; r++) {
                 int64_t e = e0 + threadIdx.x + (int64_t)r * blockDim.x;
-                if (e < t) perm[s + rank[r]] = tmp_idx[e];
+                if (e < t) {
+                    const uint32_t idx = tmp_idx[e];
+                    perm[s + rank[r]] = idx;
+                    if (out_val) {
+                        out_hi[s + rank[r]] = (int32_t)(mykey[r] >> 32);
+                        out_val[s + rank[r]] = val[idx];
+                    }
+                }
             }
         }
         __syncthreads();
@@ -96,7 +129,9 @@ __global__ void __launch_bounds__(256)
 }  // namespace
 
 int bucket_sort(const int32_t* bucket, const int64_t* skey, int64_t n, int64_t nbuckets,
-                int64_t* bucket_ptr, uint32_t* perm, unsigned* flags, cudaStream_t s) {
+                int64_t* bucket_ptr, uint32_t* perm, unsigned* flags, cudaStream_t s, const double* val,
+                int32_t* out_hi, double* out_val) {
+    if (!(val && out_hi && out_val)) val = nullptr, out_hi = nullptr, out_val = nullptr;
     (void)flags;
     RG_CHECK(n < (int64_t)UINT32_MAX, RG_ERR_UNSUPPORTED,
              "bucket_sort: %lld elements exceed the 32-bit index range", (long long)n);
@@ -121,8 +156,9 @@ int bucket_sort(const int32_t* bucket, const int64_t* skey, int64_t n, int64_t n
             unsigned g = grid_for(n, 256) > 8192 ? 8192 : grid_for(n, 256);
             scatter_buckets<<<g, 256, 0, s>>>(bucket, skey, n, bucket_ptr, counts, tmp_idx, tmp_key);
             rank_small<<<g, 256, 0, s>>>(bucket, tmp_idx, tmp_key, n, bucket_ptr, perm, long_list,
-                                         long_count);
-            rank_long<<<1024, 256, 0, s>>>(tmp_idx, tmp_key, bucket_ptr, long_list, long_count, perm);
+                                         long_count, val, out_hi, out_val);
+            rank_long<<<1024, 256, 0, s>>>(tmp_idx, tmp_key, bucket_ptr, long_list, long_count, perm, val, out_hi,
+                                           out_val);
         }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) {

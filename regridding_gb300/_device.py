@@ -43,7 +43,7 @@ def ptr(t) -> ctypes.c_void_p | None:
 # Arrays up to this size are uploaded by a kernel that reads the host array
 # (rg_copy_from_host) where the device can read pageable host memory: grids
 # and parameters then do not queue on the copy engines behind other streams'
-# large transfers (100-140 GB/s from 8 MB up on GB300).
+# large transfers (120-190 GB/s from 8 MB up on GB300).
 SM_UPLOAD_BYTES = 64 << 20
 _host_access = None
 

@@ -148,20 +148,24 @@ __device__ __forceinline__ float gs_value(float l, float r, float d, float u, co
     return __double2float_rn(dmul(dadd(dmul(k.dxxinv, xs), dmul(k.dyyinv, ys)), k.dcent));
 }
 
-// Two list entries per thread, all eight neighbour loads issued before either
-// store: cells of one class never read one another, so the order is free,
-// and the extra loads in flight hide the gather latency.
+// kFillEntries list entries per thread, all their neighbour loads issued
+// before any store: cells of one class never read one another, so the order
+// is free, and the extra loads in flight hide the gather latency.
+constexpr int kFillEntries = 2;  // 4 measured slower (86 against 82 us per iteration)
+
 template <typename T>
 __global__ void fill_update(T* __restrict__ a, const uint64_t* __restrict__ list, int64_t n, uint32_t ny,
                             FastDiv nx_div, GsConst k) {
     const uint32_t nx = nx_div.d;
     const uint64_t S = (uint64_t)ny * nx;
     const int64_t stride = (int64_t)gridDim.x * blockDim.x;
-    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += 2 * stride) {
-        T v[2][4];
-        T* dst[2] = {nullptr, nullptr};
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n; q += kFillEntries * stride) {
+        T v[kFillEntries][4];
+        T* dst[kFillEntries];
 #pragma unroll
-        for (int h = 0; h < 2; ++h) {
+        for (int h = 0; h < kFillEntries; ++h) dst[h] = nullptr;
+#pragma unroll
+        for (int h = 0; h < kFillEntries; ++h) {
             const int64_t qq = q + h * stride;
             if (qq >= n) break;
             const uint64_t e = list[qq];
@@ -178,7 +182,7 @@ __global__ void fill_update(T* __restrict__ a, const uint64_t* __restrict__ list
             dst[h] = s + c;
         }
 #pragma unroll
-        for (int h = 0; h < 2; ++h)
+        for (int h = 0; h < kFillEntries; ++h)
             if (dst[h]) *dst[h] = gs_value(v[h][0], v[h][1], v[h][2], v[h][3], k);
     }
 }

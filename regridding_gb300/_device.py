@@ -8,6 +8,7 @@ from __future__ import annotations
 
 import concurrent.futures
 import ctypes
+import mmap
 import os
 import threading
 import warnings
@@ -57,17 +58,30 @@ def kernel_host_access() -> bool:
     return _host_access
 
 
+def _file_backed(a: np.ndarray) -> bool:
+    """Whether the array's memory comes from a file mapping (np.memmap, the
+    saved weights of store.load_weights): such pages may not be resident, and
+    they are left to the copy engines rather than faulted in by a kernel."""
+    b = a
+    while b is not None:
+        if isinstance(b, (np.memmap, mmap.mmap)):
+            return True
+        b = getattr(b, "base", None)
+    return False
+
+
 def upload(a: np.ndarray, dtype=None):
     """Host array -> contiguous CUDA tensor, copied straight from the
     array's (pageable) memory: on the Grace host of a GB300 a copy-engine
     copy runs at 110-160 GB/s for arrays of 8-34 MB, twice the rate of
     staging through a pinned copy first (whose host memcpy runs at 15-25
-    GB/s); arrays up to SM_UPLOAD_BYTES go through a kernel instead."""
+    GB/s); arrays up to SM_UPLOAD_BYTES go through a kernel instead (not
+    file-mapped ones)."""
     t = torch()
     a = np.ascontiguousarray(a if dtype is None else np.asarray(a, dtype=dtype))
     if a.dtype == np.bool_:
         a = a.astype(np.uint8)
-    if 0 < a.nbytes <= SM_UPLOAD_BYTES and kernel_host_access():
+    if 0 < a.nbytes <= SM_UPLOAD_BYTES and kernel_host_access() and not _file_backed(a):
         d = t.empty(a.shape, dtype=t.from_numpy(np.empty(0, dtype=a.dtype)).dtype, device="cuda")
         _lib.call("rg_copy_from_host", ptr(d), ctypes.c_void_p(a.ctypes.data), a.nbytes, stream())
         return d

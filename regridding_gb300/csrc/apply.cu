@@ -166,6 +166,7 @@ int tiled_lists_for(rg_weights_s* W, const float* vin, cudaStream_t s, int* g, b
 int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack);
 int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made);
+int box_perm_for(rg_weights_s* W, cudaStream_t s, bool* made);
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int apply_box_exact(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s);
 int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
@@ -222,6 +223,7 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
         if (exact_box && box_usable(W, (const float*)vin, stack)) {
             RG_TRY(box_lists_for(W, s, &made));
             use_box_exact = W->box_state == 1;
+            if (use_box_exact) RG_TRY(box_perm_for(W, s, &made));
         }
         if (tiled && !use_box) RG_TRY(rows_usable(W, (const float*)vin, stack, s, &made, &use_rows));
         if (tiled && !use_box && !use_rows) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));

@@ -507,6 +507,37 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
     }
 }
 
+// Per patch, the threads' outputs for the exact apply: the patch's cells
+// sorted by row length, longest first (ties by cell), so the 32 lanes of a
+// warp run float64 chains of similar length.  A bitonic sort of 256 keys in
+// shared memory; one block per patch.
+__global__ void __launch_bounds__(PATCH * PATCH)
+    perm_patch(const int64_t* __restrict__ row_ptr, PatchGrid P, uint8_t* __restrict__ perm) {
+    __shared__ unsigned key[PATCH * PATCH];
+    const int t = threadIdx.x;
+    const int64_t p = blockIdx.x;
+    const int64_t o = patch_cell(P, p, t / PATCH, t % PATCH);
+    int64_t nk = o >= 0 ? row_ptr[o + 1] - row_ptr[o] : 0;
+    if (nk > 255) nk = 255;
+    key[t] = ((unsigned)(255 - nk) << 8) | (unsigned)t;
+    __syncthreads();
+    for (int k = 2; k <= PATCH * PATCH; k <<= 1) {
+        for (int j = k >> 1; j > 0; j >>= 1) {
+            const int ixj = t ^ j;
+            if (ixj > t) {
+                const bool up = (t & k) == 0;
+                const unsigned a = key[t], b = key[ixj];
+                if ((a > b) == up) {
+                    key[t] = b;
+                    key[ixj] = a;
+                }
+            }
+            __syncthreads();
+        }
+    }
+    perm[p * (PATCH * PATCH) + t] = (uint8_t)(key[t] & 255u);
+}
+
 // Box slot of input cell c (natural CSR order, for the exact kernel).
 __device__ __forceinline__ int box_slot_of(int c, int2 org, int64_t n1_in) {
     const int row = (int)(c / n1_in);
@@ -541,12 +572,22 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                     const double* __restrict__ dval, double* __restrict__ vout64, int64_t n1_in,
                     PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
                     unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
-                    int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags) {
+                    int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags,
+                    const uint8_t* __restrict__ perm) {
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
     extern __shared__ __align__(1024) float ring[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
-    const int64_t o = patch_cell(P, p, 4 * (warp >> 1) + (lane >> 3), 8 * (warp & 1) + (lane & 7));
+    // the thread's output: the warp tile layout, or for the exact apply the
+    // patch's outputs by row length (a warp's lanes then run chains of
+    // similar length; each chain is still summed in stored order)
+    int pr = 4 * (warp >> 1) + (lane >> 3), pc = 8 * (warp & 1) + (lane & 7);
+    if (EXACT && perm) {
+        const int raw = perm[p * (PATCH * PATCH) + t];
+        pr = raw / PATCH;
+        pc = raw % PATCH;
+    }
+    const int64_t o = patch_cell(P, p, pr, pc);
     const int64_t d0 = (int64_t)blockIdx.y * chunk;
     const int64_t d1 = d0 + chunk < stack ? d0 + chunk : stack;
     int64_t s = 0, e = 0;
@@ -1057,6 +1098,16 @@ PatchGrid patch_grid(const rg_weights_s* W) {
 // when anything was launched).  Leaves box_state -1 when the footprints do
 // not fit a box (more than 1 % of the patches, and more than 4, would need
 // direct gathers).
+// The exact apply's per-patch thread order (made once, with the box lists).
+int box_perm_for(rg_weights_s* W, cudaStream_t s, bool* made) {
+    if (W->box_perm || W->box_state != 1) return RG_OK;
+    *made = true;
+    RG_TRY(dalloc(&W->box_perm, (size_t)W->box_patches * PATCH * PATCH, s));
+    perm_patch<<<(unsigned)W->box_patches, PATCH * PATCH, 0, s>>>(W->row_ptr, patch_grid(W), W->box_perm);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
 int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
     if (W->box_state != 0) return RG_OK;
     *made = true;
@@ -1158,7 +1209,7 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     apply_patch_tma<SPS, NST, MINB, EXACT><<<grid, 32 * PATCH_WARPS, smem, s>>>(
         map, W->row_ptr, W->col, W->box_slot, W->box_val, W->val32, W->val, EXACT ? (double*)vout : nullptr,
         W->in_shape1, patch_grid(W), patches, W->box_origin, BR, stage_floats, stage_bytes, vin, W->n_in,
-        EXACT ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags);
+        EXACT ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags, EXACT ? W->box_perm : nullptr);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
 }

@@ -157,6 +157,7 @@ void free_weights(rg_weights_s* W, cudaStream_t s) {
     dfree(W->box_origin, s);
     dfree(W->box_slot, s);
     dfree(W->box_val, s);
+    dfree(W->box_perm, s);
     dfree(W->dflags, s);
     delete W;
 }
@@ -608,6 +609,7 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes) {
     for (int g = 0; g < 2; g++)
         if (w->tiled_ready[g]) b += (w->t_tiles + 1) * 8 + nnz * 2;  // list pointers + slots (lists are small)
     if (w->box_state == 1) b += w->box_patches * 8 + nnz * 6;
+    if (w->box_perm) b += w->box_patches * 256;
     *bytes = b;
     return RG_OK;
 }

@@ -195,6 +195,7 @@ struct rg_weights_s {
     int box_cfg = -1;  // configuration chosen by the autotuner (-1 not tuned, -2 none fits)
     int2* box_origin = nullptr;
     uint16_t* box_slot = nullptr;  // per entry, in the order the TMA kernel gathers them
+    uint8_t* box_perm = nullptr;   // exact apply: per patch, thread -> output (longest rows first)
     float* box_val = nullptr;      // float32 weights in that order
     unsigned* dflags = nullptr;  // device error word of the asynchronous (TMA) apply
     int rows_maxlen = -1;        // longest row (for the row kernel; -1 not known yet)

@@ -204,13 +204,18 @@ def run_quick(args, local):
     gop = workloads.perturb(go)
     dw = rg.build_conservative_2d(gi, gop)
     values = workloads.cfg2_values_torch(args.stack, args.n_in - 1)
-    out = torch.empty((args.stack, (args.n_out - 1) ** 2), dtype=torch.float32, device="cuda")
-    per, wall = time_launches(lambda: dw.apply(values, out=out, accumulate="fast"), args.steps, args.warmup,
-                              torch.cuda.current_stream(), torch)
-    b = apply_bytes(args.stack, (args.n_in - 1) ** 2, (args.n_out - 1) ** 2, dw.nnz)
-    print(json.dumps({"quick": True, "n_in": args.n_in, "n_out": args.n_out, "stack": args.stack, "nnz": dw.nnz,
-                      "bytes_per_launch": b, "kernel_ms": statistics.mean(per) * 1e3,
-                      "GB_per_s": b / statistics.mean(per) / 1e9}), flush=True)
+    res = {"quick": True, "n_in": args.n_in, "n_out": args.n_out, "stack": args.stack, "nnz": dw.nnz}
+    for mode in args.quick_modes.split(","):
+        wide = mode != "fast"
+        out = torch.empty((args.stack, (args.n_out - 1) ** 2), dtype=torch.float64 if wide else torch.float32,
+                          device="cuda")
+        per, wall = time_launches(lambda: dw.apply(values, out=out, accumulate=mode), args.steps, args.warmup,
+                                  torch.cuda.current_stream(), torch)
+        b = apply_bytes(args.stack, (args.n_in - 1) ** 2, (args.n_out - 1) ** 2, dw.nnz, b_out=8 if wide else 4,
+                        b_val=8 if wide else 4)
+        res[mode] = {"bytes_per_launch": b, "kernel_ms": round(statistics.mean(per) * 1e3, 4),
+                     "GB_per_s": round(b / statistics.mean(per) / 1e9, 1)}
+    print(json.dumps(res), flush=True)
 
 
 def run_serving(args, torch):
@@ -319,17 +324,39 @@ def run_serving(args, torch):
     for r in news:
         _util.normalize_input_output_coordinates(*r["pair"], None, None, perturb=True, seed=42)
     out["host_jitter_ms_per_new_grid"] = round((time.perf_counter() - s) / len(news) * 1e3, 2)
-    # weights of the smallest new grid of the stream against the oracle (float64)
-    r = min((r for r in reqs if r["cached"] < 0), key=lambda r: cells(r["pair"][0]))
-    from regridding_gb300 import _device
-    gi, go = r["pair"]
-    got = _device.build_conservative_2d(gi, go).export_numpy()
-    exp = oracle.weights_conservative_2d(gi, go)
-    same = all(np.array_equal(a, b) for a, b in zip(got, exp))
-    rel = 0.0 if same else float(np.max(np.abs(got[2] - exp[2]) / np.abs(exp[2]))) if got[2].shape == exp[2].shape \
-        else float("inf")
-    out["weights_check"] = {"grid_cells": cells(r["pair"][0]), "bit_identical": same, "max_rel_err": rel}
+    out["weights_check"] = served_weights_check(reqs, cells)
     return out
+
+
+def served_weights_check(reqs, cells):
+    """Weights of new grids of the served stream against the oracle (float64
+    sweep + coalesce on every host core): the new grid at every size decile
+    (0, 10, ..., 90 %) and the largest one, built as the server builds them."""
+    import oracle
+    from regridding_gb300 import _device
+
+    new = sorted((r for r in reqs if r["cached"] < 0), key=lambda r: cells(r["pair"][0]))
+    picks = sorted({int(q * (len(new) - 1) / 10) for q in range(10)} | {len(new) - 1})
+    rows = []
+    for k in picks:
+        gi, go = new[k]["pair"]
+        dw = _device.build_conservative_2d(gi, go)
+        got = dw.export_numpy()
+        dw.free()
+        exp = oracle.weights_conservative_2d(gi, go)
+        same = all(np.array_equal(a, b) for a, b in zip(got, exp))
+        if same:
+            rel = 0.0
+        elif got[2].shape == exp[2].shape and all(np.array_equal(a, b) for a, b in zip(got[:2], exp[:2])):
+            rel = float(np.max(np.abs(got[2] - exp[2]) / np.maximum(np.abs(exp[2]), 1e-300)))
+        else:
+            rel = float("inf")
+        rows.append({"side": int(gi[0].shape[0] - 1), "nnz": int(exp[2].size), "bit_identical": same,
+                     "max_rel_err": rel})
+    return {"grids": rows,
+            "summary": {"grids": len(rows), "bit_identical": sum(r["bit_identical"] for r in rows),
+                        "max_rel_err": max(r["max_rel_err"] for r in rows),
+                        "sides": [r["side"] for r in rows]}}
 
 
 def run_conservative_1d(args, torch):
@@ -612,11 +639,7 @@ def run_differentiable(args, torch):
     from regridding_gb300 import workloads
     from regridding_gb300.autograd import regrid_conservative_2d
 
-    rng = np.random.default_rng(9)
-    gi = workloads.distorted_grid(1025, 0.0, 0.02)
-    go = tuple(c + rng.normal(0, 1e-4, c.shape) for c in workloads.rect_grid(769, -0.95, 0.95))
-    c, s = np.cos(0.05), np.sin(0.05)
-    gt = (c * go[0] - s * go[1], s * go[0] + c * go[1])
+    gi, go, gt = workloads.cfg4_grids()
     g = torch.Generator(device="cuda")
     g.manual_seed(4)
     v = torch.randn((16, 1024, 1024), generator=g, device="cuda").requires_grad_(True)
@@ -649,12 +672,26 @@ def run_differentiable(args, torch):
             "checks": "tests/test_gpu_autograd.py: FD (float64, h=1e-7) and transposed-weights parity"}
 
 
+WORKLOAD = ("2048^2 -> 1536^2 conservative apply of a 64-slice float32 log-normal(3, 1) stack, float64 output "
+            "as the upstream returns (quadratic-mapped input grid, rectilinear output on [-1.05, 1.05]^2)")
+HEADLINE = "apply HBM GB/s: 2048^2 -> 1536^2 conservative weights, 64-deep float32 stack, float64 output"
+
+
+def bench_config(nnz: int) -> dict:
+    """The workload of the headline, identical in both arms."""
+    n_in_cells, n_out_cells = (N_IN - 1) ** 2, (N_OUT - 1) ** 2
+    return {"workload": WORKLOAD, "stack": STACK, "input_cells": n_in_cells, "output_cells": n_out_cells,
+            "nnz": nnz, "output_dtype": "float64",
+            "bytes_per_step": apply_bytes(STACK, n_in_cells, n_out_cells, nnz, b_out=8, b_val=8),
+            "l2": "inputs (1.07 GB) exceed L2 (129 MB); no flush"}
+
+
 def run_ours(args, world, rank, local):
     import torch
 
     import oracle
     import regridding_gb300 as rg
-    from regridding_gb300 import _device, _lib, workloads
+    from regridding_gb300 import _lib, workloads
 
     torch.cuda.set_device(local)
     stream = torch.cuda.current_stream()
@@ -691,91 +728,101 @@ def run_ours(args, world, rank, local):
         fi_ms.append((time.perf_counter() - t0) * 1e3)
     n_outside = int((oi == np.iinfo(np.int64).max).sum().item())
 
-    # --- apply, float32 accumulate (headline)
+    # --- applies: compensated float64 output (headline), fast float32, exact float64
     values = workloads.cfg2_values_torch(STACK, N_IN - 1, seed=rank)
     out32 = torch.empty((STACK, n_out_cells), dtype=torch.float32, device="cuda")
     out64 = torch.empty((STACK, n_out_cells), dtype=torch.float64, device="cuda")
+    ref64 = torch.empty((STACK, n_out_cells), dtype=torch.float64, device="cuda")
     lib = _lib.load()
     h = dw.handle
 
-    def apply_fast():
-        st = lib.rg_apply(h, ctypes.c_void_p(values.data_ptr()), _lib.RG_F32, ctypes.c_void_p(out32.data_ptr()),
-                          _lib.RG_F32, STACK, _lib.RG_ACC_FAST, s_ptr)
-        if st:
-            _lib.check(st, "rg_apply")
+    def launcher(out, dtype_out, acc):
+        vp, op = ctypes.c_void_p(values.data_ptr()), ctypes.c_void_p(out.data_ptr())
 
-    def apply_exact():
-        st = lib.rg_apply(h, ctypes.c_void_p(values.data_ptr()), _lib.RG_F32, ctypes.c_void_p(out64.data_ptr()),
-                          _lib.RG_F64, STACK, _lib.RG_ACC_EXACT, s_ptr)
-        if st:
-            _lib.check(st, "rg_apply")
+        def fn():
+            st = lib.rg_apply(h, vp, _lib.RG_F32, op, dtype_out, STACK, acc, s_ptr)
+            if st:
+                _lib.check(st, "rg_apply")
+        return fn
 
-    bytes_step = apply_bytes(STACK, n_in_cells, n_out_cells, nnz)
+    apply_comp = launcher(out64, _lib.RG_F64, _lib.RG_ACC_COMPENSATED)
+    apply_fast = launcher(out32, _lib.RG_F32, _lib.RG_ACC_FAST)
+    apply_exact = launcher(ref64, _lib.RG_F64, _lib.RG_ACC_EXACT)
+
+    cfg = bench_config(nnz)
+    bytes_step = cfg["bytes_per_step"]
+    bytes_f32 = apply_bytes(STACK, n_in_cells, n_out_cells, nnz)
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        per, wall = time_launches(apply_fast, args.steps, args.warmup, stream, torch)
+        per, wall = time_launches(apply_comp, args.steps, args.warmup, stream, torch)
     barrier(world)
     wall_max = aggregate_seconds(wall, world, device="cuda")
     value = world * bytes_step * args.steps / wall_max / 1e9
     kernel_s = statistics.mean(per)
 
-    per64, wall64 = time_launches(apply_exact, max(5, args.steps // 4), 2, stream, torch)
-    bytes64 = apply_bytes(STACK, n_in_cells, n_out_cells, nnz, b_out=8, b_val=8)
+    per32, _ = time_launches(apply_fast, max(5, args.steps), 3, stream, torch)
+    per64, _ = time_launches(apply_exact, max(5, args.steps // 4), 2, stream, torch)
 
     # --- end to end through the C ABI from page-locked host buffers
     h_in = torch.empty((STACK, n_in_cells), dtype=torch.float32, pin_memory=True)
     h_in.copy_(values)
-    h_out = torch.empty((STACK, n_out_cells), dtype=torch.float32, pin_memory=True)
+    h_out = torch.empty((STACK, n_out_cells), dtype=torch.float64, pin_memory=True)
     torch.cuda.synchronize()
 
     def apply_host():
         st = lib.rg_apply_host(h, ctypes.c_void_p(h_in.data_ptr()), _lib.RG_F32, ctypes.c_void_p(h_out.data_ptr()),
-                               _lib.RG_F32, STACK, _lib.RG_ACC_FAST, 0, s_ptr)
+                               _lib.RG_F64, STACK, _lib.RG_ACC_COMPENSATED, 0, s_ptr)
         if st:
             _lib.check(st, "rg_apply_host")
 
     e2e_steps = max(3, min(args.steps, 20))
-    per_e2e, wall_e2e = time_launches(apply_host, e2e_steps, 2, stream, torch)
+    per_e2e, wall_e2e = time_launches(apply_host, e2e_steps, 3, stream, torch)
     e2e_value = world * bytes_step * e2e_steps / aggregate_seconds(wall_e2e, world, device="cuda") / 1e9
 
-    # parity spot check of the headline output against the exact float64 result
+    # parity at full size: compensated and fast against the exact float64
+    # result (bit-identical to the upstream apply), relative per output cell
+    apply_comp()
+    apply_fast()
     apply_exact()
     torch.cuda.synchronize()
-    rel = float(((out32.double() - out64).abs() / out64.abs().clamp_min(1e-30)).max().item())
+    covered = ref64 != 0
+    denom = ref64.abs().clamp_min(1e-300)
+    rel64 = float(((out64 - ref64).abs() / denom)[covered].max().item())
+    rel32 = float(((out32.double() - ref64).abs() / denom)[covered].max().item())
+    host_same = bool(torch.equal(h_out.cuda(), out64))
     # conservation: the output total against the input weighted by the
     # fraction of each input cell the output grid covers (the transposed
     # apply of ones), per slice, relative to the input total
     ones = torch.ones((1, n_out_cells), dtype=torch.float64, device="cuda")
-    covered = dw.apply(ones, transpose=True, accumulate="exact")[0]
+    frac_in = dw.apply(ones, transpose=True, accumulate="exact")[0]
     vin64 = values.double()
-    cons = ((out64.sum(1) - vin64 @ covered).abs() / vin64.sum(1)).max().item()
-    cons_uncovered = float(1.0 - (vin64 @ covered).sum().item() / vin64.sum().item())
-    del vin64, ones, covered
+    cons = ((out64.sum(1) - vin64 @ frac_in).abs() / vin64.sum(1)).max().item()
+    cons_uncovered = float(1.0 - (vin64 @ frac_in).sum().item() / vin64.sum().item())
+    del vin64, ones, frac_in, ref64
 
     # --- CPU baseline: the oracle (C restatement of the upstream loops, all cores)
     cpu = None
     if rank == 0 and not args.no_cpu:
         ii, oo, vv = dw.export_numpy()
         host_vals = h_in.numpy()
-        sample = STACK
         ts = []
         for _ in range(2):
             t0 = time.perf_counter()
-            oracle.apply(ii, oo, vv, host_vals[:sample], n_out_cells)
+            oracle.apply(ii, oo, vv, host_vals, n_out_cells)
             ts.append(time.perf_counter() - t0)
         t_cpu = min(ts)
-        cpu = {"value": round(apply_bytes(sample, n_in_cells, n_out_cells, nnz) / t_cpu / 1e9, 3), "unit": "GB/s",
-               "cores": os.cpu_count(), "kind": "port",
-               "sample": f"full {sample}-slice apply (float64 output as upstream), best of 2, "
-                         f"{t_cpu * 1e3:.1f} ms"}
+        cpu = {"value": round(bytes_step / t_cpu / 1e9, 3), "unit": "GB/s", "cores": os.cpu_count(), "kind": "port",
+               "sample": f"the full 64-slice apply, float64 output as upstream, best of 2 ({t_cpu * 1e3:.1f} ms): "
+                         "C restatement of the upstream loop, OpenMP over the stack"}
 
     peak, peak_kind = measured_peak()
     achieved = bytes_step / kernel_s / 1e9
-    traffic = profiled_traffic("apply_kernel_f32")
+    achieved32 = bytes_f32 / statistics.mean(per32) / 1e9
+    traffic = profiled_traffic("apply_kernel_compensated")
     line = {
         "metric": METRIC,
-        "headline": "apply HBM GB/s, 2048^2 -> 1536^2 conservative weights, 64-deep float32 stack",
+        "headline": HEADLINE,
         "value": round(value, 2),
         "unit": "GB/s",
         "n_gpus": world,
@@ -785,32 +832,39 @@ def run_ours(args, world, rank, local):
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
-        "dtype": "f32",
+        "dtype": "float-float (float32 stack, float64 output)",
+        "accumulate": "compensated: products split exactly by FMA, sums as float pairs (two-sum), float64 at the "
+                      f"end; max relative error against the upstream float64 result {rel64:.2e}",
         "data": "synthetic (seeded grids and log-normal stack generated on the device)",
-        "config": {"workload": "2048^2 -> 1536^2 conservative apply, stack 64 float32 (quadratic-mapped input "
-                               "grid, rectilinear output on [-1.05, 1.05]^2)",
-                   "stack": STACK, "input_cells": n_in_cells, "output_cells": n_out_cells, "nnz": nnz,
-                   "bytes_per_step": bytes_step, "l2": "inputs (1.07 GB) exceed L2 (129 MB); no flush",
-                   "parallelism": f"replicas x{world}"},
+        "config": cfg,
+        "parallelism": f"replicas x{world}",
         "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind},
+                     "frac": round(achieved / peak, 4), "traffic": traffic, "peak_kind": peak_kind,
+                     "achieved_basis": "bytes_per_step / mean CUDA-event duration of one launch",
+                     "traffic_basis": "dram read + write bytes of one launch from the ncu capture recorded in "
+                                      "profiles/traffic.json (not measured in this run)"},
         "cpu_baseline": cpu,
         "e2e": {"value": round(e2e_value, 2), "unit": "GB/s",
-                "h2d_bytes_per_step": STACK * n_in_cells * 4, "d2h_bytes_per_step": STACK * n_out_cells * 4,
-                "ms_per_step": round(wall_e2e / e2e_steps * 1e3, 3), "path": "rg_apply_host, pinned host buffers"},
+                "h2d_bytes_per_step": STACK * n_in_cells * 4, "d2h_bytes_per_step": STACK * n_out_cells * 8,
+                "ms_per_step": round(wall_e2e / e2e_steps * 1e3, 3),
+                "path": "rg_apply_host (RG_ACC_COMPENSATED), pinned host buffers", "equals_device_result": host_same},
         "gpu_launches": args.steps,
         "clocks": clocks.summary(),
-        "apply_f64_exact": {"GB_per_s": round(bytes64 / statistics.mean(per64) / 1e9, 1),
+        "apply_f32_fast": {"GB_per_s": round(achieved32, 1), "ms": round(statistics.mean(per32) * 1e3, 4),
+                           "frac_of_measured_hbm": round(achieved32 / peak, 4), "bytes_per_step": bytes_f32,
+                           "max_rel_err_vs_f64": rel32, "note": "float32 output, float32 FMA accumulation"},
+        "apply_f64_exact": {"GB_per_s": round(bytes_step / statistics.mean(per64) / 1e9, 1),
                             "ms": round(statistics.mean(per64) * 1e3, 4),
-                            "note": "bit-identical to the upstream float64 apply"},
-        "apply_f32_max_rel_err_vs_f64": rel,
-        "conservation": {"max_rel_err_exact_f64": cons, "input_fraction_outside_output_grid": cons_uncovered},
+                            "note": "bit-identical to the upstream float64 apply (FP64-pipe bound)"},
+        "conservation": {"max_rel_err": cons, "input_fraction_outside_output_grid": cons_uncovered},
         "build": {"cells_per_s": round((n_in_cells + n_out_cells) / (min(build_ms) / 1e3), 0),
                   "ms": [round(v, 2) for v in build_ms], "nnz": nnz},
         "find_indices_2d": {"points_per_s": round(px.numel() / (min(fi_ms) / 1e3), 0),
                             "ms": [round(v, 3) for v in fi_ms], "points": int(px.numel()),
                             "outside": n_outside},
     }
+    del values, out32, out64
+    torch.cuda.empty_cache()
     if rank == 0 and args.serve_requests > 0:
         line["serving"] = run_serving(args, torch)
     if rank == 0 and not args.no_extra:
@@ -821,7 +875,33 @@ def run_ours(args, world, rank, local):
         line["interp_2d"] = run_interp(args, torch)
         line["fill"] = run_fill(args, torch)
     if rank == 0:
+        line["summary"] = summary_of(line)
         print(json.dumps(line), flush=True)
+
+
+def summary_of(line: dict) -> dict:
+    """The figures of every leg in a few hundred bytes, placed last in the
+    line so that a truncated tail of the output still holds them."""
+    s = {"apply_f64out_ms": line["ms_per_step"], "apply_f64out_frac": line["roofline"]["frac"],
+         "apply_f32_ms": line["apply_f32_fast"]["ms"], "apply_f32_frac": line["apply_f32_fast"]["frac_of_measured_hbm"],
+         "apply_exact_ms": line["apply_f64_exact"]["ms"], "build_ms": min(line["build"]["ms"]),
+         "e2e_GB_per_s": line["e2e"]["value"]}
+    srv = line.get("serving")
+    if srv:
+        s["serve_poisson_p50_p99_ms"] = [srv["poisson"]["p50_ms"], srv["poisson"]["p99_ms"]]
+        s["serve_saturated_req_s"] = srv["saturated"]["req_per_s"]
+        s["serve_plain_req_s"] = srv["plain_per_call"]["req_per_s"]
+        s["serve_speedup"] = srv["speedup_saturated_vs_plain_per_call"]
+        s["serve_weights_check"] = srv.get("weights_check", {}).get("summary")
+    if "batched" in line:
+        b = line["batched"]
+        s["batched_build_ms"] = [b["build_batched_ms"], b["build_one_by_one_ms"]]
+        s["batched_apply_graph_GB_per_s"] = b["apply_graph_GB_per_s"]
+    if "differentiable" in line:
+        s["differentiable_step_ms"] = line["differentiable"]["ms_per_step"]
+    if "multilinear_1d" in line:
+        s["multilinear_1d_GB_per_s"] = line["multilinear_1d"]["apply_GB_per_s"]
+    return s
 
 
 # ---------------------------------------------------------------------------
@@ -837,8 +917,8 @@ def run_reference(args, world, rank):
 
     gi, go = workloads.cfg2_grids(N_IN, N_OUT)
     gop = workloads.perturb(go)
-    n_in_cells = (N_IN - 1) ** 2
     n_out_cells = (N_OUT - 1) ** 2
+    n_in_cells = (N_IN - 1) ** 2
     t0 = time.perf_counter()
     raw = oracle.sweep_2d(gi, gop)
     t1 = time.perf_counter()
@@ -846,9 +926,10 @@ def run_reference(args, world, rank):
     t2 = time.perf_counter()
     del raw
     nnz = vv.size
+    cfg = bench_config(nnz)
     rng = np.random.default_rng(0)
     values = rng.lognormal(3, 1, (STACK, n_in_cells)).astype(np.float32)
-    bytes_step = apply_bytes(STACK, n_in_cells, n_out_cells, nnz)
+    bytes_step = cfg["bytes_per_step"]
     for _ in range(args.warmup):
         oracle.apply(ii, oo, vv, values, n_out_cells)
     ts = []
@@ -862,7 +943,7 @@ def run_reference(args, world, rank):
     line = {
         "metric": METRIC,
         "impl": "reference",
-        "headline": "apply HBM GB/s, 2048^2 -> 1536^2 conservative weights, 64-deep float32 stack",
+        "headline": HEADLINE,
         "value": round(value, 3),
         "unit": "GB/s",
         "n_gpus": world,
@@ -874,12 +955,11 @@ def run_reference(args, world, rank):
         "vs_baseline": None,
         "dtype": "f64",
         "data": "synthetic (seeded grids, numpy log-normal stack)",
-        "config": {"workload": "2048^2 -> 1536^2 conservative apply, stack 64 float32", "stack": STACK,
-                   "input_cells": n_in_cells, "output_cells": n_out_cells, "nnz": nnz,
-                   "bytes_per_step": bytes_step, "parallelism": f"{cores} host threads"},
+        "config": cfg,
+        "parallelism": f"{cores} host threads",
         "cpu_baseline": {"value": round(value, 3), "unit": "GB/s", "cores": cores, "kind": "port",
-                         "sample": "full 64-slice apply per step (C restatement of the upstream loops, "
-                                   "OpenMP over the stack, float64 output as upstream)"},
+                         "sample": "the full 64-slice apply per step (C restatement of the upstream loop, "
+                                   "OpenMP over the stack, float64 accumulation and output as upstream)"},
         "e2e": {"value": round(value, 3), "unit": "GB/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "build": {"cells_per_s": round((n_in_cells + n_out_cells) / (t2 - t0), 0),
                   "sweep_s": round(t1 - t0, 2), "coalesce_s": round(t2 - t1, 2), "nnz": nnz},
@@ -910,6 +990,8 @@ def main(argv=None):
     p.add_argument("--n-in", type=int, default=N_IN)
     p.add_argument("--n-out", type=int, default=N_OUT)
     p.add_argument("--stack", type=int, default=STACK)
+    p.add_argument("--quick-modes", default="fast,compensated,exact",
+                   help="with --quick: accumulation modes to time, in order")
     p.add_argument("--serve-requests", type=int, default=1000, help="requests of the served stream (0: skip)")
     p.add_argument("--serve-slots", type=int, default=16)
     p.add_argument("--serve-cobuild", type=int, default=0, help="small grids built together per build job")

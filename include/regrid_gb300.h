@@ -48,6 +48,13 @@ typedef struct CUstream_st* rg_stream_t; /* == cudaStream_t */
 /* apply accumulation modes */
 #define RG_ACC_EXACT 0 /* double, multiply then add, entries in stored order: bit-identical to upstream */
 #define RG_ACC_FAST 1  /* accumulate in the output dtype with fused multiply-add */
+/* float32 input, float64 output: every product and partial sum carried as an
+ * unevaluated pair of floats (error-free products by FMA, Knuth's two-sum) on
+ * the FP32 pipe, the pair added in double at the end.  Result within
+ * (1.1e-14 + n^2 * 3.6e-15) * sum_k |w_k x_k| of the exact sum for rows of n
+ * entries (checked to 1e-12 relative against the upstream float64 apply).
+ * Every other dtype combination computes as RG_ACC_EXACT. */
+#define RG_ACC_COMPENSATED 2
 
 /* multilinear bounds (upstream `bounds` argument) */
 #define RG_BOUNDS_EXTRAPOLATE 0

@@ -46,16 +46,19 @@ def ptr(t) -> ctypes.c_void_p | None:
 # and parameters then do not queue on the copy engines behind other streams'
 # large transfers (120-190 GB/s from 8 MB up on GB300).
 SM_UPLOAD_BYTES = 64 << 20
-_host_access = None
+_host_access: dict[int, bool] = {}
 
 
 def kernel_host_access() -> bool:
-    global _host_access
-    if _host_access is None:
+    """Whether kernels on the current device may read pageable host memory
+    (asked once per device: the devices of one process can differ)."""
+    dev = torch().cuda.current_device()
+    v = _host_access.get(dev)
+    if v is None:
         out = np.zeros(3, np.int64)
         _lib.call("rg_device_attributes", ctypes.c_void_p(out.ctypes.data), 3)
-        _host_access = bool(out[2])
-    return _host_access
+        v = _host_access[dev] = bool(out[2])
+    return v
 
 
 def _file_backed(a: np.ndarray) -> bool:
@@ -214,9 +217,14 @@ class DeviceWeights:
 
         ``accumulate="exact"`` reproduces the upstream float64 result bit for
         bit (float64 output, or an upstream-style in-place float32 ``out``);
-        ``"fast"`` accumulates in the output dtype with FMA.
+        ``"fast"`` accumulates in the output dtype with FMA; ``"compensated"``
+        gives a float64 output within 1e-12 relative of the exact sum
+        (float32 input: float-float arithmetic on the FP32 pipe; other dtypes
+        compute as ``"exact"``).
         """
         t = torch()
+        if accumulate not in _lib.RG_ACC:
+            raise ValueError(f"accumulate must be one of {sorted(_lib.RG_ACC)}, got {accumulate!r}")
         n_src, n_dst = (self.n_out, self.n_in) if transpose else (self.n_in, self.n_out)
         squeeze = values.dim() == 1
         v = values.reshape(-1, n_src)
@@ -226,13 +234,10 @@ class DeviceWeights:
             v = v.to(t.float64)
         stack = v.shape[0]
         if out is None:
-            if accumulate == "exact":
-                odt = t.float64
-            else:
-                odt = v.dtype
+            odt = v.dtype if accumulate == "fast" else t.float64
             out = t.empty((stack, n_dst), dtype=odt, device="cuda")
         o = out.reshape(stack, n_dst)
-        acc = _lib.RG_ACC_EXACT if accumulate == "exact" else _lib.RG_ACC_FAST
+        acc = _lib.RG_ACC[accumulate]
         dt_in = _lib.RG_F32 if v.dtype == t.float32 else _lib.RG_F64
         dt_out = _lib.RG_F32 if o.dtype == t.float32 else _lib.RG_F64
         fn = "rg_apply_transpose" if transpose else "rg_apply"

@@ -26,6 +26,8 @@ RG_FILL_GUESS_SLICE = 1
 RG_FILL_GUESS_FULL = 2
 RG_ACC_EXACT = 0
 RG_ACC_FAST = 1
+RG_ACC_COMPENSATED = 2
+RG_ACC = {"exact": RG_ACC_EXACT, "fast": RG_ACC_FAST, "compensated": RG_ACC_COMPENSATED}
 RG_BOUNDS = {"extrapolate": 0, "nan": 1, "raise": 2}
 
 _P = ctypes.c_void_p

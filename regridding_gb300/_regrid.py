@@ -47,7 +47,7 @@ def regrid_from_weights(
     axis_input: None | int | Sequence[int] = None,
     axis_output: None | int | Sequence[int] = None,
     *,
-    accumulate: Literal["exact", "fast"] = "exact",
+    accumulate: Literal["exact", "fast", "compensated"] = "exact",
 ) -> np.ndarray:
     """Apply saved weights to an array (drop-in for ``regridding.regrid_from_weights``).
 
@@ -56,8 +56,13 @@ def regrid_from_weights(
     float32 result).  ``accumulate="fast"`` accumulates in the output dtype
     with FMA (float32 output for float32 input unless ``values_output`` says
     otherwise): the HBM-bandwidth path, within about 1e-6 relative of the
-    float64 result.
+    float64 result.  ``accumulate="compensated"`` returns the upstream's
+    float64 output within 1e-12 relative of it, computed for float32 input
+    in float-float arithmetic at close to the fast path's speed (other
+    inputs compute as ``"exact"``).
     """
+    if accumulate not in ("exact", "fast", "compensated"):
+        raise ValueError(f"accumulate must be 'exact', 'fast' or 'compensated', got {accumulate!r}")
     unit = getattr(values_input, "unit", None)
     if unit is not None:
         values_input = getattr(values_input, "value")
@@ -181,7 +186,7 @@ def regrid(
     perturb: None | bool = None,
     seed: "None | int | np.random.Generator" = _util.SEED_DEFAULT,
     *,
-    accumulate: Literal["exact", "fast"] = "exact",
+    accumulate: Literal["exact", "fast", "compensated"] = "exact",
 ) -> np.ndarray:
     """Regrid in one call (drop-in for ``regridding.regrid``).
 

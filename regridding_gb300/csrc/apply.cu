@@ -129,9 +129,10 @@ int apply_csr(const int64_t* row_ptr, const int32_t* col, const double* val, con
               cudaStream_t s) {
     RG_CHECK(dtype_in == RG_F32 || dtype_in == RG_F64, RG_ERR_ARG, "apply: bad input dtype");
     RG_CHECK(dtype_out == RG_F32 || dtype_out == RG_F64, RG_ERR_ARG, "apply: bad output dtype");
-    RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST, RG_ERR_ARG, "apply: bad accumulation mode");
+    RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST || acc == RG_ACC_COMPENSATED, RG_ERR_ARG,
+             "apply: bad accumulation mode");
     if (stack <= 0 || n_rows <= 0) return RG_OK;
-    if (acc == RG_ACC_EXACT) {
+    if (acc != RG_ACC_FAST) {  // exact, or compensated where the staged kernel does not take the call
         if (dtype_out == RG_F64) {
             if (dtype_in == RG_F32)
                 return launch<float, double, 0, double>(row_ptr, col, val, n_rows, shape0, shape1, vin, n_cols,
@@ -167,9 +168,12 @@ int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int
 bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack);
 int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made);
 int box_perm_for(rg_weights_s* W, cudaStream_t s, bool* made);
+int ff_lists_for(rg_weights_s* W, cudaStream_t s, bool* made);
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int apply_box_exact(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s);
-int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int apply_box_ff(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s);
+int tune_box_fast(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
+int tune_box_ff(rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s);
 int rows_usable(rg_weights_s* W, const float* vin, int64_t stack, cudaStream_t s, bool* made, bool* ok);
 int apply_rows_launch(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s);
 int ensure_transposed(rg_weights_s* W, cudaStream_t s);
@@ -183,7 +187,8 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
                   int dtype_out, int64_t stack, int acc, cudaStream_t s) {
     RG_CHECK(dtype_in == RG_F32 || dtype_in == RG_F64, RG_ERR_ARG, "apply: bad input dtype");
     RG_CHECK(dtype_out == RG_F32 || dtype_out == RG_F64, RG_ERR_ARG, "apply: bad output dtype");
-    RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST, RG_ERR_ARG, "apply: bad accumulation mode");
+    RG_CHECK(acc == RG_ACC_EXACT || acc == RG_ACC_FAST || acc == RG_ACC_COMPENSATED, RG_ERR_ARG,
+             "apply: bad accumulation mode");
     if (stack <= 0) return RG_OK;
     // the bandwidth path: float32 in and out, input staged in shared memory (by
     // tensor-map copies when the input grid shape allows, else by the warps)
@@ -192,10 +197,13 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
     // the exact float64 apply of a float32 stack stages input boxes too
     const bool exact_box = !transposed && acc == RG_ACC_EXACT && dtype_in == RG_F32 && dtype_out == RG_F64 &&
                            W->n_out > 0 && W->nnz > 0;
+    // the compensated apply: float32 stack, float64 output, float-float sums
+    const bool ff_box = !transposed && acc == RG_ACC_COMPENSATED && dtype_in == RG_F32 && dtype_out == RG_F64 &&
+                        W->n_out > 0 && W->nnz > 0;
     // (the patch lists keep a float32 copy of the weights in gather order)
-    const bool need32 = ((acc == RG_ACC_FAST && dtype_out == RG_F32) || exact_box) && W->nnz > 0;
+    const bool need32 = ((acc == RG_ACC_FAST && dtype_out == RG_F32) || exact_box || ff_box) && W->nnz > 0;
     int g = 0;
-    bool use_box = false, use_rows = false, use_box_exact = false;
+    bool use_box = false, use_rows = false, use_box_exact = false, use_box_ff = false;
     {
         std::lock_guard<std::mutex> lock(W->mu);
         bool made = false;
@@ -216,7 +224,7 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
             if (use_box && W->box_cfg == -1) {
                 if (made) RG_CUDA(cudaStreamSynchronize(s));
                 made = false;
-                RG_TRY(tune_box(W, (const float*)vin, (float*)vout, stack, s));
+                RG_TRY(tune_box_fast(W, (const float*)vin, (float*)vout, stack, s));
             }
             use_box = use_box && W->box_cfg >= 0;
         }
@@ -225,6 +233,17 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
             use_box_exact = W->box_state == 1;
             if (use_box_exact) RG_TRY(box_perm_for(W, s, &made));
         }
+        if (ff_box && box_usable(W, (const float*)vin, stack)) {
+            RG_TRY(box_lists_for(W, s, &made));
+            use_box_ff = W->box_state == 1;
+            if (use_box_ff) RG_TRY(ff_lists_for(W, s, &made));
+            if (use_box_ff && W->box_cfg_ff == -1) {
+                if (made) RG_CUDA(cudaStreamSynchronize(s));
+                made = false;
+                RG_TRY(tune_box_ff(W, (const float*)vin, (double*)vout, stack, s));
+            }
+            use_box_ff = use_box_ff && W->box_cfg_ff >= 0;
+        }
         if (tiled && !use_box) RG_TRY(rows_usable(W, (const float*)vin, stack, s, &made, &use_rows));
         if (tiled && !use_box && !use_rows) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));
         if (made) RG_CUDA(cudaStreamSynchronize(s));
@@ -232,6 +251,10 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
     if (use_rows) return apply_rows_launch(W, (const float*)vin, (float*)vout, stack, s);
     if (use_box_exact) {
         const int st = apply_box_exact(W, (const float*)vin, (double*)vout, stack, s);
+        if (st != RG_ERR_UNSUPPORTED) return st;
+    }
+    if (use_box_ff) {
+        const int st = apply_box_ff(W, (const float*)vin, (double*)vout, stack, s);
         if (st != RG_ERR_UNSUPPORTED) return st;
     }
     if (use_box) {

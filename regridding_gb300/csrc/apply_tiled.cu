@@ -23,6 +23,7 @@
 #include <algorithm>
 #include <climits>
 #include <map>
+#include <tuple>
 #include <cstdio>
 #include <cstdlib>
 
@@ -435,45 +436,79 @@ __global__ void __launch_bounds__(256)
     }
 }
 
+// Box slot of input cell c (the slot prepare_patch gives it).
+__device__ __forceinline__ int box_slot_of(int c, int2 org, int64_t n1_in) {
+    const int row = (int)(c / n1_in);
+    const int r = row - org.x, cc = (int)(c - (int64_t)row * n1_in) - org.y;
+    return r * PBOX_C + ((((cc >> 2) ^ (r & 7)) << 2) | (cc & 3));
+}
+
+// The part of a float64 weight that its float32 rounding hi = (float)w
+// misses, rounded to float32: w - hi is exact in double (hi is w rounded to
+// 24 bits), and hi + lo carries 48 bits of w (|w - hi - lo| <= 2^-48 |w|).
+__device__ __forceinline__ float weight_rest(double w, float hi) {
+    return __double2float_rn(__dsub_rn(w, (double)hi));
+}
+
 // Order of every lane's entries in the TMA kernel.  At step k each lane of
 // a warp gathers its k-th entry; two lanes whose cells are different words
 // of the same shared-memory bank (slot mod 32; the per-slice swizzle phase
 // flips every lane's bank alike) are served one after the other, while lanes
-// reading the same word share one access.  One warp per warp tile, laid out
-// as in the apply kernel: for every step, lane by lane, each lane takes a
-// remaining entry whose word an earlier lane reads at this step, else one
-// whose bank no earlier lane uses, else its first remaining entry.
-// (Neighbouring output cells share input cells, so shared words are common:
-// on the 1024^2 -> 768^2 weights this takes the gathers from 1.81 to 1.56
-// accesses per step.)  Writes the reordered slots and float32 weights (the
-// CSR itself, which fixes the exact paths' order, is unchanged).  Lanes with
-// more than ORDER_MAX entries keep the stored order.
+// reading the same word share one access.  One block per patch, its threads
+// laid out as in the apply kernel that will read the order (perm null: the
+// warp tiles of the fast kernel; else thread t takes patch cell perm[t], the
+// row-length order of the compensated kernel): for every step, lane by lane,
+// each lane takes a remaining entry whose word an earlier lane reads at this
+// step, else one whose bank no earlier lane uses, else its first remaining
+// entry.  (Neighbouring output cells share input cells, so shared words are
+// common: on the 1024^2 -> 768^2 weights this takes the warp tiles' gathers
+// from 1.81 to 1.56 accesses per step.)  The entries' natural slots come from
+// slot_in, or from their columns when it is null; writes the reordered
+// slots, float32 weights and (lo_out non-null) the weights' float32 rests.
+// The CSR itself, which fixes the exact paths' order, is unchanged.  Lanes
+// with more than ORDER_MAX entries keep the stored order.
 constexpr int ORDER_MAX = 16;
 
 __global__ void __launch_bounds__(32 * PATCH_WARPS)
-    order_patch(const int64_t* __restrict__ row_ptr, const float* __restrict__ val32, PatchGrid P,
-                const int2* __restrict__ origin, uint16_t* __restrict__ slot, float* __restrict__ box_val) {
+    order_patch(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, int64_t n1_in,
+                const float* __restrict__ val32, const double* __restrict__ val, PatchGrid P,
+                const int2* __restrict__ origin, const uint8_t* __restrict__ perm, const uint16_t* slot_in,
+                uint16_t* slot_out, float* __restrict__ hi_out, float* __restrict__ lo_out) {
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
-    const int64_t o = patch_cell(P, p, 4 * (warp >> 1) + (lane >> 3), 8 * (warp & 1) + (lane & 7));
+    int pr = 4 * (warp >> 1) + (lane >> 3), pc = 8 * (warp & 1) + (lane & 7);
+    if (perm) {
+        const int raw = perm[p * (PATCH * PATCH) + t];
+        pr = raw / PATCH;
+        pc = raw % PATCH;
+    }
+    const int64_t o = patch_cell(P, p, pr, pc);
     int64_t s = 0, e = 0;
     if (o >= 0) {
         s = row_ptr[o];
         e = row_ptr[o + 1];
     }
     const int nk = (int)(e - s);
-    const bool boxed = origin[p].x >= 0;
-    if (!boxed) return;  // block-uniform
+    const int2 org = origin[p];
+    if (org.x < 0) return;  // block-uniform
+    auto natural = [&](int64_t k) -> uint16_t {
+        return slot_in ? slot_in[k] : (uint16_t)box_slot_of(col[k], org, n1_in);
+    };
     if (nk > ORDER_MAX) {
-        for (int64_t k = s; k < e; k++) box_val[k] = val32[k];
+        for (int64_t k = s; k < e; k++) {
+            slot_out[k] = natural(k);
+            hi_out[k] = val32[k];
+            if (lo_out) lo_out[k] = weight_rest(val[k], val32[k]);
+        }
         // keep the stored order, but the other lanes still take part below
     }
     uint16_t sl[ORDER_MAX];
-    float vl[ORDER_MAX];
+    float vl[ORDER_MAX], vr[ORDER_MAX];
     const int mine = nk <= ORDER_MAX ? nk : 0;
     for (int k = 0; k < ORDER_MAX; k++) {
-        sl[k] = k < mine ? slot[s + k] : 0;
+        sl[k] = k < mine ? natural(s + k) : 0;
         vl[k] = k < mine ? val32[s + k] : 0.f;
+        vr[k] = (k < mine && lo_out) ? weight_rest(val[s + k], vl[k]) : 0.f;
     }
     unsigned left = mine == 32 ? 0xffffffffu : ((1u << mine) - 1u);  // entries not yet placed
     int kmax = mine;
@@ -497,8 +532,9 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
                 for (int c = 0; c < ORDER_MAX; c++)
                     if (c == pick) {
                         if (owner[warp][sl[c] & 31] == 0xffffu) owner[warp][sl[c] & 31] = sl[c];
-                        slot[s + k] = sl[c];
-                        box_val[s + k] = vl[c];
+                        slot_out[s + k] = sl[c];
+                        hi_out[s + k] = vl[c];
+                        if (lo_out) lo_out[s + k] = vr[c];
                     }
             }
             __syncwarp();
@@ -538,51 +574,92 @@ __global__ void __launch_bounds__(PATCH * PATCH)
     perm[p * (PATCH * PATCH) + t] = (uint8_t)(key[t] & 255u);
 }
 
-// Box slot of input cell c (natural CSR order, for the exact kernel).
-__device__ __forceinline__ int box_slot_of(int c, int2 org, int64_t n1_in) {
-    const int row = (int)(c / n1_in);
-    const int r = row - org.x, cc = (int)(c - (int64_t)row * n1_in) - org.y;
-    return r * PBOX_C + ((((cc >> 2) ^ (r & 7)) << 2) | (cc & 3));
-}
-
-// float32 -> float64, exactly, on the integer pipe: for a normal binary32
-// value the binary64 value has the same sign, the exponent rebiased from 127
-// to 1023 and the 23 fraction bits followed by 29 zeros.  Zeros, subnormals,
-// infinities and NaNs take the hardware conversion.  (The exact apply spends
-// most of its FP64 issue slots on its multiply and add; this keeps the
-// conversion off that pipe.)
+// float32 -> float64, exactly, with integer operations only (the FP64 pipe
+// of a GB300 issues 2 operations per clock per SM and is kept for the sums):
+// a normal binary32 value keeps its sign, its exponent is rebiased from 127
+// to 1023 and its 23 fraction bits are followed by 29 zeros; a subnormal
+// man * 2^-149 is normalised at its leading bit; zeros keep their sign;
+// infinities and NaNs keep their payload under the all-ones exponent.
 __device__ __forceinline__ double widen(float f) {
     const unsigned u = __float_as_uint(f);
-    const unsigned ex = (u >> 23) & 0xffu;
-    if (ex == 0u || ex == 0xffu) return (double)f;
-    const unsigned long long bits = ((unsigned long long)(u >> 31) << 63) |
-                                    ((unsigned long long)(ex + (1023u - 127u)) << 52) |
-                                    ((unsigned long long)(u & 0x7fffffu) << 29);
-    return __longlong_as_double((long long)bits);
+    const unsigned ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
+    unsigned long long e64 = 0ull, m64 = 0ull;
+    if (ex != 0u) {
+        e64 = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex + (1023u - 127u));
+        m64 = (unsigned long long)man << 29;
+    } else if (man != 0u) {
+        const int lead = 31 - __clz((int)man);  // 0..22
+        e64 = (unsigned long long)(lead + 1023 - 149);
+        m64 = ((unsigned long long)man << (52 - lead)) & 0xfffffffffffffull;
+    }
+    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (e64 << 52) | m64));
 }
 
-// EXACT: the upstream float64 apply bit for bit (float32 input, float64
-// weights and output): every entry in stored (CSR) order as
-// acc = acc + w * (double)x with one rounding per operation, from 0.0.
-template <int SPS, int NST, int MINB, bool EXACT>
+// Whether a float32 is finite, from its exponent bits.
+__device__ __forceinline__ bool finite_bits(float f) {
+    return (__float_as_uint(f) & 0x7f800000u) != 0x7f800000u;
+}
+
+// Whether a float32 is normal (neither zero, subnormal, infinite nor NaN).
+__device__ __forceinline__ bool normal_bits(unsigned u) {
+    return (u & 0x7f800000u) - 0x00800000u < 0x7f000000u;
+}
+
+// widen() of a normal float32, from its bits: the double's high word is the
+// sign, the exponent rebiased by 1023 - 127 and the top 20 fraction bits;
+// the low word the last 3 fraction bits.
+__device__ __forceinline__ double widen_normal(unsigned u) {
+    const unsigned hi = (u & 0x80000000u) | (((u & 0x7fffffffu) >> 3) + ((1023u - 127u) << 20));
+    return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// Accumulation modes of the TMA apply.
+//  MODE_FAST:  float32 output, acc = fmaf(w, x, acc) with float32 weights in
+//              the bank-aware gather order.
+//  MODE_EXACT: the upstream float64 apply bit for bit (float32 input, float64
+//              weights and output): every entry in stored (CSR) order as
+//              acc = acc + w * (double)x with one rounding per operation, from 0.0.
+//  MODE_FF:    float64 output from float-float arithmetic on the FP32 pipe
+//              (the GB300 runs FP32 at 64x its FP64 rate): each weight as
+//              hi + lo floats, each product x * hi split exactly into p + e
+//              by an FMA (Dekker's product), the running sum kept as an
+//              unevaluated pair (h, l) with Knuth's two-sum, and h + l added
+//              in double once per output.  Entries in the gather order.
+constexpr int MODE_FAST = 0, MODE_EXACT = 1, MODE_FF = 2;
+
+// One float-float step: (h, l) += x * (wh + wl).
+__device__ __forceinline__ void ff_step(float& h, float& l, float wh, float wl, float x) {
+    const float p = __fmul_rn(x, wh);
+    const float e = __fmaf_rn(x, wh, -p);      // x * wh - p, exactly
+    const float r = __fmaf_rn(x, wl, e);       // the product's low part
+    const float t = __fadd_rn(h, p);           // two-sum of h and p: t + err = h + p exactly
+    const float bp = __fsub_rn(t, h);
+    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+    h = t;
+    l = __fadd_rn(l, __fadd_rn(err, r));
+}
+
+template <int SPS, int NST, int MINB, int MODE, int CT = CACHED_T>
 __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     apply_patch_tma(const __grid_constant__ CUtensorMap tmap, const int64_t* __restrict__ row_ptr,
                     const int32_t* __restrict__ col, const uint16_t* __restrict__ slot,
-                    const float* __restrict__ bval, const float* __restrict__ val,
+                    const float* __restrict__ bval, const float* __restrict__ blo, const float* __restrict__ val,
                     const double* __restrict__ dval, double* __restrict__ vout64, int64_t n1_in,
                     PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
                     unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
                     int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags,
                     const uint8_t* __restrict__ perm) {
+    constexpr bool EXACT = MODE == MODE_EXACT;
+    constexpr bool OUT64 = MODE != MODE_FAST;
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
     extern __shared__ __align__(1024) float ring[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
-    // the thread's output: the warp tile layout, or for the exact apply the
-    // patch's outputs by row length (a warp's lanes then run chains of
-    // similar length; each chain is still summed in stored order)
+    // the thread's output: the warp tile layout, or for the exact and
+    // compensated applies the patch's outputs by row length (a warp's lanes
+    // then run chains of similar length)
     int pr = 4 * (warp >> 1) + (lane >> 3), pc = 8 * (warp & 1) + (lane & 7);
-    if (EXACT && perm) {
+    if (OUT64 && perm) {
         const int raw = perm[p * (PATCH * PATCH) + t];
         pr = raw / PATCH;
         pc = raw % PATCH;
@@ -601,7 +678,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     if (org.x < 0) {
         // no entries (all zeros) or a footprint larger than the box: the whole block
         if (o >= 0) {
-            if constexpr (EXACT) {
+            if constexpr (OUT64) {
                 for (int64_t d = d0; d < d1; d++) {
                     const float* a = vin + d * n_in;
                     double acc = 0.0;
@@ -619,18 +696,21 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     // multiple of 4, odd slices see the pattern shifted by 4 rows, which is
     // the chunk index xor 4 (slot xor 16)
     const int flip = (BR & 4) ? 16 : 0;
-    int li[CACHED_T];
-    float w[CACHED_T];
-    double wd[CACHED_T];
+    // (CT = 0 keeps a single dummy slot: every entry is read from memory)
+    int li[CT > 0 ? CT : 1];
+    float w[CT > 0 ? CT : 1], wl[CT > 0 ? CT : 1];
+    double wd[CT > 0 ? CT : 1];
 #pragma unroll
-    for (int k = 0; k < CACHED_T; k++) {
+    for (int k = 0; k < CT; k++) {
         if constexpr (EXACT) {
             li[k] = k < nk ? box_slot_of(col[s + k], org, n1_in) : 0;
             wd[k] = k < nk ? dval[s + k] : 0.0;
             w[k] = 0.f;
+            wl[k] = 0.f;
         } else {
             li[k] = k < nk ? (int)slot[s + k] : 0;
             w[k] = k < nk ? bval[s + k] : 0.f;
+            wl[k] = (MODE == MODE_FF && k < nk) ? blo[s + k] : 0.f;
             wd[k] = 0.0;
         }
     }
@@ -668,7 +748,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
 #pragma unroll
                 for (int q = 0; q < SPS; q++) acc[q] = 0.0;
 #pragma unroll
-                for (int k = 0; k < CACHED_T; k++) {
+                for (int k = 0; k < CT; k++) {
                     if (k < nk) {
 #pragma unroll
                         for (int q = 0; q < SPS; q++)
@@ -676,7 +756,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                                 acc[q], __dmul_rn(wd[k], widen(buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))])));
                     }
                 }
-                for (int64_t k = s + CACHED_T; k < e; k++) {
+                for (int64_t k = s + CT; k < e; k++) {
                     const double wk = dval[k];
                     const int sk = box_slot_of(col[k], org, n1_in);
 #pragma unroll
@@ -687,19 +767,62 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                 for (int q = 0; q < SPS; q++)
                     if (ds + q < d1) vout64[(ds + q) * n_out + o] = acc[q];
             }
+        } else if constexpr (MODE == MODE_FF) {
+            if (o >= 0) {
+                float h[SPS], l[SPS];
+#pragma unroll
+                for (int q = 0; q < SPS; q++) h[q] = l[q] = 0.f;
+#pragma unroll
+                for (int k = 0; k < CT; k++) {
+                    if (k < nk) {
+#pragma unroll
+                        for (int q = 0; q < SPS; q++)
+                            ff_step(h[q], l[q], w[k], wl[k], buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))]);
+                    }
+                }
+                for (int64_t k = s + CT; k < e; k++) {
+                    const float wk = bval[k], wlk = blo[k];
+                    const int sk = slot[k];
+#pragma unroll
+                    for (int q = 0; q < SPS; q++)
+                        ff_step(h[q], l[q], wk, wlk, buf[q * plane + (sk ^ ((q & 1) ? flip : 0))]);
+                }
+#pragma unroll
+                for (int q = 0; q < SPS; q++) {
+                    if (ds + q >= d1) continue;
+                    double r;
+                    const unsigned uh = __float_as_uint(h[q]), ul = __float_as_uint(l[q]);
+                    if (normal_bits(uh) && normal_bits(ul)) {
+                        r = __dadd_rn(widen_normal(uh), widen_normal(ul));
+                    } else if (nk == 0) {
+                        r = 0.0;
+                    } else if (finite_bits(h[q]) && finite_bits(l[q])) {
+                        r = __dadd_rn(widen(h[q]), widen(l[q]));
+                    } else {
+                        // a float32 partial sum overflowed, or an input or a
+                        // weight is not finite: this output and slice in
+                        // float64, stored order (the exact apply's sum)
+                        r = 0.0;
+                        for (int64_t k = s; k < e; k++)
+                            r = __dadd_rn(r, __dmul_rn(dval[k], widen(buf[q * plane + (box_slot_of(col[k], org, n1_in) ^
+                                                                                     ((q & 1) ? flip : 0))])));
+                    }
+                    vout64[(ds + q) * n_out + o] = r;
+                }
+            }
         } else if (o >= 0) {
             float acc[SPS];
 #pragma unroll
             for (int q = 0; q < SPS; q++) acc[q] = 0.f;
 #pragma unroll
-            for (int k = 0; k < CACHED_T; k++) {
+            for (int k = 0; k < CT; k++) {
                 if (k < nk) {
 #pragma unroll
                     for (int q = 0; q < SPS; q++)
                         acc[q] = fmaf(w[k], buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))], acc[q]);
                 }
             }
-            for (int64_t k = s + CACHED_T; k < e; k++) {
+            for (int64_t k = s + CT; k < e; k++) {
                 const float wk = bval[k];
                 const int sk = slot[k];
 #pragma unroll
@@ -1080,7 +1203,7 @@ int apply_tiled(const rg_weights_s* W, int g, const float* vin, float* vout, int
 // Whether the TMA apply can take this call: output and input grid shapes
 // known, input rows of whole 16-byte chunks, 16-byte aligned slices.
 bool box_usable(const rg_weights_s* W, const float* vin, int64_t stack) {
-    return W->box_state >= 0 && W->box_cfg != -2 && W->out_shape0 > 0 && W->out_shape1 > 0 &&
+    return W->box_state >= 0 && W->out_shape0 > 0 && W->out_shape1 > 0 &&
            W->out_shape0 * W->out_shape1 == W->n_out && W->in_shape0 > 0 && W->in_shape1 > 0 &&
            W->in_shape1 % 4 == 0 && W->in_shape0 * W->in_shape1 == W->n_in && ((uintptr_t)vin & 15) == 0 &&
            stack >= 1 && W->n_in < INT32_MAX && stack < INT32_MAX && encode_tiled() != nullptr;
@@ -1106,6 +1229,38 @@ int box_perm_for(rg_weights_s* W, cudaStream_t s, bool* made) {
     perm_patch<<<(unsigned)W->box_patches, PATCH * PATCH, 0, s>>>(W->row_ptr, patch_grid(W), W->box_perm);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
+}
+
+// The compensated apply's entry order (made once, after the box lists):
+// threads take the patch's outputs by row length (box_perm), and every
+// lane's entries are ordered for that layout with their float32 weights and
+// the weights' float32 rests.
+int ff_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
+    if (W->ff_slot || W->box_state != 1) return RG_OK;
+    RG_TRY(box_perm_for(W, s, made));
+    *made = true;
+    int st = RG_OK;
+    do {
+        if ((st = dalloc(&W->ff_slot, (size_t)W->nnz, s))) break;
+        if ((st = dalloc(&W->ff_hi, (size_t)W->nnz, s))) break;
+        if ((st = dalloc(&W->ff_lo, (size_t)W->nnz, s))) break;
+        order_patch<<<(unsigned)W->box_patches, 32 * PATCH_WARPS, 0, s>>>(
+            W->row_ptr, W->col, W->in_shape1, W->val32, W->val, patch_grid(W), W->box_origin, W->box_perm, nullptr,
+            W->ff_slot, W->ff_hi, W->ff_lo);
+        if (cudaGetLastError() != cudaSuccess) {
+            set_error("apply (compensated lists): launch failed");
+            st = RG_ERR_CUDA;
+        }
+    } while (0);
+    if (st != RG_OK) {
+        dfree(W->ff_slot, s);
+        dfree(W->ff_hi, s);
+        dfree(W->ff_lo, s);
+        W->ff_slot = nullptr;
+        W->ff_hi = nullptr;
+        W->ff_lo = nullptr;
+    }
+    return st;
 }
 
 int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
@@ -1152,8 +1307,9 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         W->box_cols = PBOX_C;
         W->box_patches = patches;
         if ((st = dalloc(&W->box_val, (size_t)W->nnz, s))) break;
-        order_patch<<<(unsigned)patches, 32 * PATCH_WARPS, 0, s>>>(W->row_ptr, W->val32, P, W->box_origin,
-                                                                   W->box_slot, W->box_val);
+        order_patch<<<(unsigned)patches, 32 * PATCH_WARPS, 0, s>>>(W->row_ptr, W->col, W->in_shape1, W->val32,
+                                                                   W->val, P, W->box_origin, nullptr, W->box_slot,
+                                                                   W->box_slot, W->box_val, nullptr);
         const bool few = (int64_t)h[2] * 100 <= patches || h[2] <= 4;  // patches left to direct gathers
         W->box_state = few && BR <= W->in_shape0 && PBOX_C <= W->in_shape1 ? 1 : -1;
     } while (0);
@@ -1180,8 +1336,17 @@ struct BoxConfig {
 };
 constexpr BoxConfig kBoxConfigs[] = {{4, 2, 0}, {4, 2, 4}, {4, 3, 4}, {2, 3, 4}, {2, 4, 4}, {8, 2, 0}, {4, 3, 0}};
 constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]));
+// The compensated kernel's configurations add the number of entries a
+// thread keeps in registers (fewer registers, more resident blocks); forced
+// by RG_APPLY_FF_CONFIG="sps,nst,minb,cached".
+struct FFConfig {
+    int sps, nst, minb, cached;
+};
+constexpr FFConfig kFFConfigs[] = {{4, 2, 0, 8}, {4, 3, 3, 4}, {8, 2, 3, 4}, {4, 3, 3, 0},
+                                   {8, 2, 2, 8}, {2, 4, 4, 0}, {4, 2, 4, 0}};
+constexpr int kNumFFConfigs = (int)(sizeof(kFFConfigs) / sizeof(kFFConfigs[0]));
 
-template <int SPS, int NST, int MINB, bool EXACT = false>
+template <int SPS, int NST, int MINB, int MODE = MODE_FAST, int CT = CACHED_T>
 int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, const float* vin, void* vout,
                  int64_t stack, cudaStream_t s) {
     const int BR = W->box_rows;
@@ -1191,7 +1356,7 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     if (smem > 200 * 1024) return RG_ERR_UNSUPPORTED;
     static std::once_flag attr;
     std::call_once(attr, []() {
-        cudaFuncSetAttribute(apply_patch_tma<SPS, NST, MINB, EXACT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaFuncSetAttribute(apply_patch_tma<SPS, NST, MINB, MODE, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              200 * 1024);
         cudaGetLastError();
     });
@@ -1206,10 +1371,13 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     if ((stack + chunk - 1) / chunk > 65535) chunk = ((stack + 65534) / 65535 + SPS - 1) / SPS * SPS;
     const int64_t nchunks = (stack + chunk - 1) / chunk;
     dim3 grid((unsigned)patches, (unsigned)nchunks);
-    apply_patch_tma<SPS, NST, MINB, EXACT><<<grid, 32 * PATCH_WARPS, smem, s>>>(
-        map, W->row_ptr, W->col, W->box_slot, W->box_val, W->val32, W->val, EXACT ? (double*)vout : nullptr,
-        W->in_shape1, patch_grid(W), patches, W->box_origin, BR, stage_floats, stage_bytes, vin, W->n_in,
-        EXACT ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags, EXACT ? W->box_perm : nullptr);
+    constexpr bool OUT64 = MODE != MODE_FAST;
+    constexpr bool FF = MODE == MODE_FF;
+    apply_patch_tma<SPS, NST, MINB, MODE, CT><<<grid, 32 * PATCH_WARPS, smem, s>>>(
+        map, W->row_ptr, W->col, FF ? W->ff_slot : W->box_slot, FF ? W->ff_hi : W->box_val, FF ? W->ff_lo : nullptr,
+        W->val32, W->val, OUT64 ? (double*)vout : nullptr, W->in_shape1, patch_grid(W), patches, W->box_origin, BR,
+        stage_floats, stage_bytes, vin, W->n_in, OUT64 ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags,
+        OUT64 ? W->box_perm : nullptr);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
 }
@@ -1226,7 +1394,9 @@ bool encode_stack(const rg_weights_s* W, const float* vin, int64_t stack, int bs
                           CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
-int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+template <int MODE>
+int launch_box_config_mode(const rg_weights_s* W, int cfg, const float* vin, void* vout, int64_t stack,
+                           cudaStream_t s) {
     const BoxConfig c = kBoxConfigs[cfg];
     // a stack shorter than a stage: the box carries only its slices (the
     // stage's other slices are never stored)
@@ -1234,18 +1404,53 @@ int launch_box_config(const rg_weights_s* W, int cfg, const float* vin, float* v
     CUtensorMap map;
     if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
-        case 0: return launch_patch<4, 2, 0>(W, map, bs, vin, vout, stack, s);
-        case 1: return launch_patch<4, 2, 4>(W, map, bs, vin, vout, stack, s);
-        case 2: return launch_patch<4, 3, 4>(W, map, bs, vin, vout, stack, s);
-        case 3: return launch_patch<2, 3, 4>(W, map, bs, vin, vout, stack, s);
-        case 4: return launch_patch<2, 4, 4>(W, map, bs, vin, vout, stack, s);
-        case 5: return launch_patch<8, 2, 0>(W, map, bs, vin, vout, stack, s);
-        case 6: return launch_patch<4, 3, 0>(W, map, bs, vin, vout, stack, s);
+        case 0: return launch_patch<4, 2, 0, MODE>(W, map, bs, vin, vout, stack, s);
+        case 1: return launch_patch<4, 2, 4, MODE>(W, map, bs, vin, vout, stack, s);
+        case 2: return launch_patch<4, 3, 4, MODE>(W, map, bs, vin, vout, stack, s);
+        case 3: return launch_patch<2, 3, 4, MODE>(W, map, bs, vin, vout, stack, s);
+        case 4: return launch_patch<2, 4, 4, MODE>(W, map, bs, vin, vout, stack, s);
+        case 5: return launch_patch<8, 2, 0, MODE>(W, map, bs, vin, vout, stack, s);
+        case 6: return launch_patch<4, 3, 0, MODE>(W, map, bs, vin, vout, stack, s);
     }
     return RG_ERR_UNSUPPORTED;
 }
 
-int forced_box_config() {
+int launch_ff_config(const rg_weights_s* W, int cfg, const float* vin, void* vout, int64_t stack, cudaStream_t s) {
+    const FFConfig c = kFFConfigs[cfg];
+    const int bs = (int)std::min<int64_t>(c.sps, stack);
+    CUtensorMap map;
+    if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
+    switch (cfg) {
+        case 0: return launch_patch<4, 2, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
+        case 1: return launch_patch<4, 3, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
+        case 2: return launch_patch<8, 2, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
+        case 3: return launch_patch<4, 3, 3, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
+        case 4: return launch_patch<8, 2, 2, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
+        case 5: return launch_patch<2, 4, 4, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
+        case 6: return launch_patch<4, 2, 4, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
+    }
+    return RG_ERR_UNSUPPORTED;
+}
+
+// MODE_FAST (float32 vout, kBoxConfigs) or MODE_FF (float64 vout, kFFConfigs).
+int launch_box_config(const rg_weights_s* W, int mode, int cfg, const float* vin, void* vout, int64_t stack,
+                      cudaStream_t s) {
+    if (mode == MODE_FF) return launch_ff_config(W, cfg, vin, vout, stack, s);
+    return launch_box_config_mode<MODE_FAST>(W, cfg, vin, vout, stack, s);
+}
+
+int forced_box_config(int mode) {
+    if (mode == MODE_FF) {
+        const char* env = getenv("RG_APPLY_FF_CONFIG");
+        if (!env) return -1;
+        int a = 0, b = 0, c = 0, d = 0;
+        if (sscanf(env, "%d,%d,%d,%d", &a, &b, &c, &d) != 4) return -1;
+        for (int k = 0; k < kNumFFConfigs; k++)
+            if (kFFConfigs[k].sps == a && kFFConfigs[k].nst == b && kFFConfigs[k].minb == c &&
+                kFFConfigs[k].cached == d)
+                return k;
+        return -1;
+    }
     const char* env = getenv("RG_APPLY_BOX_CONFIG");
     if (!env) return -1;
     int a = 0, b = 0, c = 0;
@@ -1263,7 +1468,7 @@ int forced_box_config() {
 // Tuned configurations shared by handles of the same kind: box height and
 // stack size class (1, 2-3, 4-7, ..., 64+) -> configuration.
 std::mutex g_tuned_mutex;
-std::map<std::pair<int, int>, int> g_tuned;
+std::map<std::tuple<int, int, int>, int> g_tuned;  // (mode, box rows, stack class) -> configuration
 
 int stack_class(int64_t stack) {
     int c = 0;
@@ -1271,19 +1476,20 @@ int stack_class(int64_t stack) {
     return c;
 }
 
-int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
-    if (W->box_cfg >= 0) return RG_OK;
-    const int forced = forced_box_config();
+int tune_box(rg_weights_s* W, int mode, const float* vin, void* vout, int64_t stack, cudaStream_t s) {
+    int& chosen = mode == MODE_FF ? W->box_cfg_ff : W->box_cfg;
+    if (chosen >= 0) return RG_OK;
+    const int forced = forced_box_config(mode);
     if (forced >= 0) {
-        W->box_cfg = forced;
+        chosen = forced;
         return RG_OK;
     }
-    const std::pair<int, int> kind(W->box_rows, stack_class(stack));
+    const std::tuple<int, int, int> kind(mode, W->box_rows, stack_class(stack));
     {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         auto it = g_tuned.find(kind);
         if (it != g_tuned.end()) {
-            W->box_cfg = it->second;
+            chosen = it->second;
             return RG_OK;
         }
     }
@@ -1297,15 +1503,16 @@ int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cuda
     int best = -1;
     float best_ms = 0;
     int st = RG_OK;
-    for (int k = 0; k < kNumBoxConfigs && st == RG_OK; k++) {
-        if (launch_box_config(W, k, vin, vout, stack, s) != RG_OK) {  // warm-up; skips configs that do not fit
+    const int ncfg = mode == MODE_FF ? kNumFFConfigs : kNumBoxConfigs;
+    for (int k = 0; k < ncfg && st == RG_OK; k++) {
+        if (launch_box_config(W, mode, k, vin, vout, stack, s) != RG_OK) {  // warm-up; skips configs that do not fit
             cudaGetLastError();
             continue;
         }
         float ms = 0;
         for (int rep = 0; rep < 2; rep++) {
             cudaEventRecord(e0, s);
-            launch_box_config(W, k, vin, vout, stack, s);
+            launch_box_config(W, mode, k, vin, vout, stack, s);
             cudaEventRecord(e1, s);
             if (cudaEventSynchronize(e1) != cudaSuccess) {
                 set_error("apply (tuning): %s", cudaGetErrorString(cudaGetLastError()));
@@ -1324,7 +1531,7 @@ int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cuda
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (st != RG_OK) return st;
-    W->box_cfg = best >= 0 ? best : -2;
+    chosen = best >= 0 ? best : -2;
     if (best >= 0) {
         std::lock_guard<std::mutex> lock(g_tuned_mutex);
         g_tuned[kind] = best;
@@ -1337,7 +1544,21 @@ int tune_box(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cuda
 // another kernel.
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
     if (W->box_cfg < 0) return RG_ERR_UNSUPPORTED;
-    return launch_box_config(W, W->box_cfg, vin, vout, stack, s);
+    return launch_box_config(W, MODE_FAST, W->box_cfg, vin, vout, stack, s);
+}
+
+// The compensated (float-float) TMA apply with its tuned configuration.
+int apply_box_ff(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s) {
+    if (W->box_state != 1 || W->box_cfg_ff < 0 || !W->ff_slot || !W->box_perm) return RG_ERR_UNSUPPORTED;
+    return launch_box_config(W, MODE_FF, W->box_cfg_ff, vin, vout, stack, s);
+}
+
+int tune_box_fast(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
+    return tune_box(W, MODE_FAST, vin, vout, stack, s);
+}
+
+int tune_box_ff(rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s) {
+    return tune_box(W, MODE_FF, vin, vout, stack, s);
 }
 
 // The exact (float64) TMA apply: 4 slices per stage, 2 stages (FP64 issue,
@@ -1347,7 +1568,7 @@ int apply_box_exact(const rg_weights_s* W, const float* vin, double* vout, int64
     const int bs = (int)std::min<int64_t>(4, stack);
     CUtensorMap map;
     if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
-    return launch_patch<4, 2, 0, true>(W, map, bs, vin, vout, stack, s);
+    return launch_patch<4, 2, 0, MODE_EXACT>(W, map, bs, vin, vout, stack, s);
 }
 
 // Whether the row kernel can take this call (the caller holds the lock and

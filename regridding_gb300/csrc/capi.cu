@@ -157,6 +157,9 @@ void free_weights(rg_weights_s* W, cudaStream_t s) {
     dfree(W->box_origin, s);
     dfree(W->box_slot, s);
     dfree(W->box_val, s);
+    dfree(W->ff_slot, s);
+    dfree(W->ff_hi, s);
+    dfree(W->ff_lo, s);
     dfree(W->box_perm, s);
     dfree(W->dflags, s);
     delete W;
@@ -236,23 +239,31 @@ __global__ void zero_bytes(unsigned char* __restrict__ p, size_t n) {
     }
 }
 
-int g_host_access = -1;  // -1: not queried yet
+constexpr int kMaxDevices = 64;
+int g_host_access[kMaxDevices];  // per device ordinal: 0 not queried yet, 1 yes, 2 no
 std::mutex g_host_access_mu;
 
 }  // namespace
 
+// Whether kernels on the CURRENT device may dereference pageable host
+// pointers (queried once per device ordinal: devices of one process can
+// differ).
 bool kernel_host_access() {
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+        cudaGetLastError();
+        return false;
+    }
     std::lock_guard<std::mutex> lock(g_host_access_mu);
-    if (g_host_access < 0) {
-        int dev = 0, v = 0;
-        if (cudaGetDevice(&dev) != cudaSuccess ||
-            cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
+    if (g_host_access[dev] == 0) {
+        int v = 0;
+        if (cudaDeviceGetAttribute(&v, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess) {
             cudaGetLastError();
             v = 0;
         }
-        g_host_access = v ? 1 : 0;
+        g_host_access[dev] = v ? 1 : 2;
     }
-    return g_host_access == 1;
+    return g_host_access[dev] == 1;
 }
 
 static unsigned small_blocks(size_t n) {
@@ -608,7 +619,8 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes) {
     if (w->t_val32) b += nnz * 4;
     for (int g = 0; g < 2; g++)
         if (w->tiled_ready[g]) b += (w->t_tiles + 1) * 8 + nnz * 2;  // list pointers + slots (lists are small)
-    if (w->box_state == 1) b += w->box_patches * 8 + nnz * 6;
+    if (w->box_state == 1) b += w->box_patches * 8 + nnz * 6;  // origins; slot and float32 weight per entry
+    if (w->ff_slot) b += nnz * 10;                              // compensated: slot, hi and lo per entry
     if (w->box_perm) b += w->box_patches * 256;
     *bytes = b;
     return RG_OK;

@@ -197,6 +197,13 @@ struct rg_weights_s {
     uint16_t* box_slot = nullptr;  // per entry, in the order the TMA kernel gathers them
     uint8_t* box_perm = nullptr;   // exact apply: per patch, thread -> output (longest rows first)
     float* box_val = nullptr;      // float32 weights in that order
+    // the compensated (float-float) apply: per entry its box slot, float32
+    // weight hi = (float)w and rest lo = (float)(w - hi), in the order its
+    // row-length thread layout (box_perm) gathers them; its tuned configuration
+    uint16_t* ff_slot = nullptr;
+    float* ff_hi = nullptr;
+    float* ff_lo = nullptr;
+    int box_cfg_ff = -1;
     unsigned* dflags = nullptr;  // device error word of the asynchronous (TMA) apply
     int rows_maxlen = -1;        // longest row (for the row kernel; -1 not known yet)
     int device = 0;

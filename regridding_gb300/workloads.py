@@ -83,6 +83,21 @@ def cfg2_values_torch(stack: int = 64, n: int = 2048, seed: int = 0, device="cud
     return v.exp_()
 
 
+def cfg4_grids(n_in: int = 1025, n_out: int = 769, seed: int = 9):
+    """The differentiable-regrid workload: input ``n_in x n_in`` vertices on
+    [-1, 1]^2 with sinusoidal distortion of amplitude 0.02 (no rotation);
+    output a rectilinear ``n_out x n_out`` grid on [-0.95, 0.95]^2 plus
+    N(0, 1e-4) vertex jitter (the initial value of the learnable output
+    coordinates); the target grid is the output grid rotated by 0.05 rad.
+    Returns (grid_input, grid_output, grid_target)."""
+    rng = np.random.default_rng(seed)
+    gi = distorted_grid(n_in, 0.0, 0.02)
+    go = tuple(c + rng.normal(0, 1e-4, c.shape) for c in rect_grid(n_out, -0.95, 0.95))
+    c, s = np.cos(0.05), np.sin(0.05)
+    gt = (c * go[0] - s * go[1], s * go[0] + c * go[1])
+    return gi, go, gt
+
+
 def grid_pair(rng: np.random.Generator, side: int, jitter: bool = True):
     """One grid pair of the batched and served configurations: an input of
     ``side x side`` cells on [-1, 1]^2 with a random rotation in [0, 0.5) rad

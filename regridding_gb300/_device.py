@@ -344,11 +344,29 @@ def build_conservative_2d_batch(pairs, weights_input=None, max_cells: int = 48_0
 
 # ---------------------------------------------------------------------------
 # device-resident copies of saved weights, keyed by the identity of their
-# (read-only) numpy arrays
+# numpy arrays; writable arrays (which the caller may have edited since)
+# also by a hash of their contents
 # ---------------------------------------------------------------------------
 
 _cache_lock = threading.Lock()
 _cache: dict[tuple, tuple] = {}
+
+
+def content_hash(a: np.ndarray) -> tuple:
+    """dtype, shape and two seeded 64-bit hashes of the array's bytes, taken
+    in one pass on up to 16 host threads (rg_hash64x2)."""
+    a = np.ascontiguousarray(a)
+    h = (ctypes.c_uint64 * 2)()
+    _lib.call("rg_hash64x2", ctypes.c_void_p(a.ctypes.data), a.nbytes, 0x5EED, 0xC0FFEE, h)
+    return (a.dtype.str, a.shape, int(h[0]), int(h[1]))
+
+
+def _fingerprint(element: tuple):
+    """None for an element whose three arrays are read-only (the identity
+    of the arrays is its key); else the content hashes of the three."""
+    if all(not a.flags.writeable for a in element):
+        return None
+    return tuple(content_hash(a) for a in element)
 
 
 def _drop(key: tuple) -> None:
@@ -357,27 +375,33 @@ def _drop(key: tuple) -> None:
 
 
 def remember(element: tuple, dw: DeviceWeights) -> None:
-    """Associate the device copy with a saved-layout element whose arrays are read-only."""
+    """Associate the device copy with a saved-layout element (numpy arrays).
+    Read-only arrays are recognised by identity; writable ones by identity
+    and contents, so an element edited in place is uploaded again."""
     ii, oo, vv = element
-    if not all(isinstance(a, np.ndarray) and not a.flags.writeable for a in (ii, oo, vv)):
+    if not all(isinstance(a, np.ndarray) for a in (ii, oo, vv)):
         return
     key = (id(ii), id(oo), id(vv))
+    fp = _fingerprint(element)
     with _cache_lock:
-        _cache[key] = (weakref.ref(ii), weakref.ref(oo), weakref.ref(vv), dw)
+        _cache[key] = (weakref.ref(ii), weakref.ref(oo), weakref.ref(vv), dw, fp)
     weakref.finalize(vv, _drop, key)
 
 
 def lookup(element: tuple, n_in: int, n_out: int) -> DeviceWeights | None:
     ii, oo, vv = element
-    if not isinstance(vv, np.ndarray):
+    if not all(isinstance(a, np.ndarray) for a in (ii, oo, vv)):
         return None
     with _cache_lock:
         hit = _cache.get((id(ii), id(oo), id(vv)))
     if hit is None:
         return None
-    ri, ro, rv, dw = hit
+    ri, ro, rv, dw, fp = hit
     if ri() is not ii or ro() is not oo or rv() is not vv:
         return None
-    if vv.flags.writeable or dw.n_in != n_in or dw.n_out != n_out:
+    if dw.n_in != n_in or dw.n_out != n_out:
         return None
-    return dw
+    if fp is None:
+        # remembered read-only: still read-only means unchanged
+        return dw if all(not a.flags.writeable for a in element) else None
+    return dw if _fingerprint(element) == fp else None

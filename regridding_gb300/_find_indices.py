@@ -47,12 +47,13 @@ def find_indices(
     ci = tuple(np.moveaxis(v, axi, numba_in).reshape(-1, *shape_in_numba) for v in ci)
     co = tuple(np.moveaxis(v, axo, numba_out).reshape(-1, *shape_out_numba) for v in co)
 
-    if method not in ("brute", "searchsorted", "exhaustive"):
+    # "exhaustive" exists only for the 2D extension; in 1D the upstream knows
+    # "brute" and "searchsorted" and rejects every other name
+    # (regridding/_find_indices/_find_indices.py:112-125)
+    if method not in ("brute", "searchsorted", "exhaustive") or (method == "exhaustive" and len(ci) == 1):
         raise ValueError(f"method `{method}` not recognized.")
 
     if len(ci) == 1:
-        if method == "exhaustive":
-            method = "brute"
         result = (_find_1d(ci[0], co[0], int(fill_value), method),)
     elif len(ci) == 2:
         if method == "searchsorted":

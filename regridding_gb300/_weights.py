@@ -76,21 +76,14 @@ def _weights_device(coordinates_input, coordinates_output, axis_input, axis_outp
 
 
 def _elements(nd: int, h_in, h_out, h_val, counts) -> np.ndarray:
-    """The saved layout's elements as read-only views of the first
-    ``counts[d]`` entries of row ``d`` of the downloaded (nd, cap) arrays:
-    no per-element copy (10^5 spectra of ~1,800 entries are 4.3 GB)."""
-    for a in (h_in, h_out, h_val):
-        a.flags.writeable = False
+    """The saved layout's elements as views of the first ``counts[d]``
+    entries of row ``d`` of the downloaded (nd, cap) arrays: no per-element
+    copy (10^5 spectra of ~1,800 entries are 4.3 GB).  Writable, as the
+    upstream's arrays are."""
     flat = np.empty(nd, dtype=object)
     for d, c in enumerate(counts):
         flat[d] = (h_in[d, :c], h_out[d, :c], h_val[d, :c])
     return flat
-
-
-def _freeze(*arrays):
-    for a in arrays:
-        a.flags.writeable = False
-    return arrays
 
 
 def _rows(a: np.ndarray, axes, last: int):
@@ -158,7 +151,7 @@ def _conservative(ci, co, axis_input, axis_output, weights_input, perturb, seed,
             None if w_index is None else np.ascontiguousarray(w_index, dtype=float),
         )
         if want_host:
-            element = _freeze(*dw.export_numpy())
+            element = tuple(dw.export_numpy())
             _device.remember(element, dw)
             array[index] = element
         dev.append(dw)

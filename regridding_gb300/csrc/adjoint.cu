@@ -17,9 +17,11 @@
 // s = d - c, n = (-s.y, s.x) / cross(r, s).
 //
 // One thread per output cell: for every stored entry (i, o) it forms
-// dL/dw_io = sum_d grad_out[d, o] * values[d, i], multiplies by dw/dA and adds
-// the 8 coordinate derivatives of its quad into the gradient arrays
-// (double atomics).
+// dL/dw_io = sum_d grad_out[d, o] * values[d, i], multiplies by dw/dA and
+// sums the 8 coordinate derivatives of its quad over its entries (in stored
+// order) into a per-cell record; a second kernel gives every output vertex
+// the sum of its (up to four) cells' corner terms in a fixed order, so the
+// gradient is the same bits on every run (no atomics).
 #include "common.cuh"
 
 namespace rg {
@@ -117,7 +119,7 @@ __global__ void __launch_bounds__(128)
                        const double* __restrict__ yi, int64_t nyi, const double* __restrict__ xo,
                        const double* __restrict__ yo, int64_t nyo, const double* __restrict__ area_in,
                        const double* __restrict__ w_in, const T* __restrict__ values, const T* __restrict__ gout,
-                       int64_t n_in, int64_t stack, double* __restrict__ gx, double* __restrict__ gy,
+                       int64_t n_in, int64_t stack, double* __restrict__ corner,
                        double* __restrict__ w_check, unsigned* __restrict__ flags) {
     const int64_t o = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     if (o >= n_out) return;
@@ -126,7 +128,6 @@ __global__ void __launch_bounds__(128)
     Quad O;
     load_quad(xo, yo, nyo, io, jo, O);
     double ax[4] = {0, 0, 0, 0}, ay[4] = {0, 0, 0, 0};
-    bool any = false;
     for (int64_t k = row_ptr[o]; k < row_ptr[o + 1]; k++) {
         const int64_t i = col[k];
         double G = 0;
@@ -209,14 +210,34 @@ __global__ void __launch_bounds__(128)
                 ay[b] += q.t * hy;
             }
         }
-        any = true;
     }
-    if (!any) return;
-    const int64_t vid[4] = {io * nyo + jo, (io + 1) * nyo + jo, (io + 1) * nyo + jo + 1, io * nyo + jo + 1};
+    double* rec = corner + o * 8;
     for (int v = 0; v < 4; v++) {
-        if (ax[v] != 0) atomicAdd(gx + vid[v], ax[v]);
-        if (ay[v] != 0) atomicAdd(gy + vid[v], ay[v]);
+        rec[v] = ax[v];
+        rec[4 + v] = ay[v];
     }
+}
+
+// Gradient of output vertex (a, b): corner 0 of cell (a, b), corner 1 of
+// cell (a - 1, b), corner 2 of cell (a - 1, b - 1) and corner 3 of cell
+// (a, b - 1), those that exist, added in that order.
+__global__ void __launch_bounds__(256)
+    vertex_sum(const double* __restrict__ corner, int64_t nxo, int64_t nyo, double* __restrict__ gx,
+               double* __restrict__ gy) {
+    const int64_t v = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (v >= nxo * nyo) return;
+    const int64_t a = v / nyo, b = v - a * nyo, ncy = nyo - 1;
+    double sx = 0.0, sy = 0.0;
+    const int64_t ci[4] = {a, a - 1, a - 1, a};
+    const int64_t cj[4] = {b, b, b - 1, b - 1};
+    for (int c = 0; c < 4; c++) {
+        if (ci[c] < 0 || ci[c] >= nxo - 1 || cj[c] < 0 || cj[c] >= ncy) continue;
+        const double* rec = corner + (ci[c] * ncy + cj[c]) * 8;
+        sx += rec[c];
+        sy += rec[4 + c];
+    }
+    gx[v] = sx;
+    gy[v] = sy;
 }
 
 }  // namespace
@@ -241,14 +262,18 @@ extern "C" int rg_conservative_2d_grad_output(rg_weights w, const double* d_xi, 
     RG_CHECK(stack >= 0, RG_ERR_ARG, "rg_conservative_2d_grad_output: negative stack");
     cudaStream_t s = (cudaStream_t)stream;
     const int64_t nv = nxo * nyo;
-    RG_CUDA(cudaMemsetAsync(d_grad_xo, 0, sizeof(double) * nv, s));
-    RG_CUDA(cudaMemsetAsync(d_grad_yo, 0, sizeof(double) * nv, s));
-    if (w->n_out == 0 || w->nnz == 0) return RG_OK;
+    if (w->n_out == 0 || w->nnz == 0) {
+        RG_CUDA(cudaMemsetAsync(d_grad_xo, 0, sizeof(double) * nv, s));
+        RG_CUDA(cudaMemsetAsync(d_grad_yo, 0, sizeof(double) * nv, s));
+        return RG_OK;
+    }
     double* area = nullptr;
+    double* corner = nullptr;
     unsigned* flags = nullptr;
     int st = RG_OK;
     do {
         if ((st = dalloc(&area, (size_t)w->n_in, s))) break;
+        if ((st = dalloc(&corner, (size_t)w->n_out * 8, s))) break;
         if ((st = dalloc(&flags, 1, s))) break;
         cudaMemsetAsync(flags, 0, sizeof(unsigned), s);
         if ((st = cell_area_2d(d_xi, d_yi, nxi, nyi, area, s))) break;
@@ -256,13 +281,12 @@ extern "C" int rg_conservative_2d_grad_output(rg_weights w, const double* d_xi, 
         if (dtype == RG_F32)
             grad_output_kernel<float><<<grid, 128, 0, s>>>(
                 w->row_ptr, w->col, w->val, w->n_out, d_xi, d_yi, nyi, d_xo, d_yo, nyo, area, d_w_in,
-                (const float*)d_values, (const float*)d_grad_out, w->n_in, stack, d_grad_xo, d_grad_yo, d_w_check,
-                flags);
+                (const float*)d_values, (const float*)d_grad_out, w->n_in, stack, corner, d_w_check, flags);
         else
             grad_output_kernel<double><<<grid, 128, 0, s>>>(
                 w->row_ptr, w->col, w->val, w->n_out, d_xi, d_yi, nyi, d_xo, d_yo, nyo, area, d_w_in,
-                (const double*)d_values, (const double*)d_grad_out, w->n_in, stack, d_grad_xo, d_grad_yo,
-                d_w_check, flags);
+                (const double*)d_values, (const double*)d_grad_out, w->n_in, stack, corner, d_w_check, flags);
+        vertex_sum<<<grid_for(nv, 256), 256, 0, s>>>(corner, nxo, nyo, d_grad_xo, d_grad_yo);
         unsigned fl = 0;
         cudaMemcpyAsync(&fl, flags, sizeof(unsigned), cudaMemcpyDeviceToHost, s);
         cudaError_t e = cudaStreamSynchronize(s);
@@ -281,6 +305,7 @@ extern "C" int rg_conservative_2d_grad_output(rg_weights w, const double* d_xi, 
         }
     } while (0);
     dfree(area, s);
+    dfree(corner, s);
     dfree(flags, s);
     return st;
 }

@@ -57,11 +57,7 @@ _key_memo_lock = threading.Lock()
 
 
 def _hash_array(a: np.ndarray) -> tuple:
-    a = np.ascontiguousarray(a)
-    h = (ctypes.c_uint64 * 2)()
-    # two seeded 64-bit hashes in one pass over the array
-    _lib.call("rg_hash64x2", ctypes.c_void_p(a.ctypes.data), a.nbytes, 0x5EED, 0xC0FFEE, h)
-    return (a.dtype.str, a.shape, int(h[0]), int(h[1]))
+    return _device.content_hash(a)
 
 
 def _forget(memo: tuple) -> None:

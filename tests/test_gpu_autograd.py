@@ -148,3 +148,24 @@ def test_nonconvex_input_cells_are_refused(torch):
     out = regrid_conservative_2d(torch.ones((1, 8, 8), dtype=torch.float64).cuda(), (x, y), (xo, yo))
     with pytest.raises(_lib.RegridError, match="convex"):
         out.sum().backward()
+
+
+def test_coordinate_gradient_is_deterministic(torch):
+    """The coordinate gradient has no atomics: every output vertex sums its
+    cells' corner terms in a fixed order, so repeated backward passes give
+    the same bits (a 129^2 -> 97^2 case, many cells per vertex row)."""
+    from regridding_gb300.autograd import regrid_conservative_2d
+
+    gi, go, rng = problem(129, 97, seed=6)
+    v = torch.from_numpy(rng.normal(0, 1, (3, 128, 128))).cuda()
+    g = torch.from_numpy(rng.normal(0, 1, (3, 96, 96))).cuda()
+    grads = []
+    for _ in range(3):
+        xo = torch.from_numpy(go[0].copy()).cuda().requires_grad_(True)
+        yo = torch.from_numpy(go[1].copy()).cuda().requires_grad_(True)
+        regrid_conservative_2d(v, gi, (xo, yo)).backward(g)
+        grads.append((xo.grad.cpu().numpy(), yo.grad.cpu().numpy()))
+    for gx, gy in grads[1:]:
+        np.testing.assert_array_equal(gx, grads[0][0])
+        np.testing.assert_array_equal(gy, grads[0][1])
+    assert np.abs(grads[0][0]).max() > 0

@@ -368,7 +368,7 @@ def run_conservative_1d(args, torch):
     import regridding_gb300 as rg
 
     rng = np.random.default_rng(14)
-    nd, m, n = 100_000, 1025, 769
+    nd, m, n = (10_000 if getattr(args, "small", False) else 100_000), 1025, 769
     x_in = np.sort(rng.uniform(0, 1, (nd, m)), axis=1)
     x_out = np.sort(rng.uniform(0, 1, (nd, n)), axis=1)
     ts = []
@@ -384,7 +384,7 @@ def run_conservative_1d(args, torch):
     for k in range(1000):
         oracle.conservative_1d(x_in[k], x_out[k])
     t_cpu = time.perf_counter() - t0
-    return {"workload": "1D conservative, 10^5 spectra, 1025 -> 769 edges each, per-spectrum grids",
+    return {"workload": f"1D conservative, {nd} spectra, 1025 -> 769 edges each, per-spectrum grids",
             "weights_ms": round(min(ts) * 1e3, 1), "spectra_per_s": round(nd / min(ts), 0),
             "bit_identical_to_oracle_sample": same,
             "cpu_baseline": {"spectra_per_s": round(1000 / t_cpu, 0), "cores": 1, "kind": "port",
@@ -401,7 +401,7 @@ def run_batched(args, torch):
     from regridding_gb300 import _device, batching, workloads
 
     t0 = time.perf_counter()
-    pairs, stacks = workloads.batched_pairs(256)
+    pairs, stacks = workloads.batched_pairs(32 if getattr(args, "small", False) else 256)
     t_gen = time.perf_counter() - t0
     cells = sum((gi[0].shape[0] - 1) * (gi[0].shape[1] - 1) + (go[0].shape[0] - 1) * (go[0].shape[1] - 1)
                 for gi, go in pairs)
@@ -456,7 +456,7 @@ def run_batched(args, torch):
 
     t_eager = timed(graph.eager)
     t_graph = timed(graph.replay)
-    return {"workload": "256 uneven grid pairs, sides 64-1024 cells, stacks {1, 4, 16} float32 Poisson(50)",
+    return {"workload": f"{len(pairs)} uneven grid pairs, sides 64-1024 cells, stacks {{1, 4, 16}} float32 Poisson(50)",
             "input_plus_output_cells": cells, "generation_s": round(t_gen, 2), "failed_pairs": failed,
             "build_batched_ms": round(t_batch * 1e3, 2), "build_one_by_one_ms": round(t_single * 1e3, 2),
             "build_batched_cells_per_s": round(cells / t_batch, 0),
@@ -484,7 +484,7 @@ def run_multilinear_1d(args, torch):
     t_w = time.perf_counter() - t0
     ii, oo, vv = w[()] if w.shape == () else w.reshape(-1)[0]
     dw = _device.DeviceWeights.from_coo(ii, oo, vv, 4096, 4096)
-    n_spec = 1_000_000
+    n_spec = 50_000 if getattr(args, "small", False) else 1_000_000
     g = torch.Generator(device="cuda")
     g.manual_seed(13)
     vals = torch.rand((n_spec, 4096), generator=g, device="cuda", dtype=torch.float32)
@@ -502,7 +502,7 @@ def run_multilinear_1d(args, torch):
     oracle.apply(ii, oo, vv, host, 4096)
     t_cpu = time.perf_counter() - t0
     del vals, out
-    return {"workload": "1D multilinear, 4096 -> 4096 samples, 10^6 float32 spectra", "nnz": int(dw.nnz),
+    return {"workload": f"1D multilinear, 4096 -> 4096 samples, {n_spec} float32 spectra", "nnz": int(dw.nnz),
             "weights_ms": round(t_w * 1e3, 2), "apply_ms": round(statistics.mean(per) * 1e3, 3),
             "apply_GB_per_s": round(nbytes / statistics.mean(per) / 1e9, 1),
             "spectra_per_s": round(n_spec / statistics.mean(per), 0), "max_rel_err_vs_f64_sample": rel,
@@ -626,6 +626,35 @@ def run_fill(args, torch):
             "public_call_ms": round(t_public * 1e3, 1), "bit_identical_to_oracle_slice": same,
             "cpu_baseline": {"cell_updates_per_s": round(int(where[0].sum()) * iters / t_cpu, 0), "cores": 1,
                              "kind": "port", "sample": f"one 1024^2 slice, {iters} iterations, sequential C"}}
+
+
+def run_find_indices_2d(args, torch):
+    """2D find_indices (the lowest-index input cell holding each point) of
+    the output vertices of the 2048^2 -> 1536^2 grids (sizes from --n-in and
+    --n-out) by the grid walk, on resident device arrays; a 20,000-point
+    sample is checked against the oracle's secant locate."""
+    import oracle
+    import regridding_gb300 as rg
+    from regridding_gb300 import workloads
+
+    gi, go = workloads.cfg2_grids(args.n_in, args.n_out)
+    gop = workloads.perturb(go)
+    d_gi = tuple(torch.from_numpy(np.ascontiguousarray(a)).cuda() for a in gi)
+    px = torch.from_numpy(np.ascontiguousarray(gop[0]).reshape(-1)).cuda()
+    py = torch.from_numpy(np.ascontiguousarray(gop[1]).reshape(-1)).cuda()
+    ts = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        oi, oj = rg.locate_2d(d_gi, px, py, method="brute")
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    pick = np.random.default_rng(1).choice(px.numel(), 20_000, replace=False)
+    exp = oracle.locate(gi, gop[0].reshape(-1)[pick], gop[1].reshape(-1)[pick], "secant")
+    same = bool(np.array_equal(oi.cpu().numpy()[pick], exp[0]) and np.array_equal(oj.cpu().numpy()[pick], exp[1]))
+    return {"workload": f"{px.numel()} output vertices in the {args.n_in - 1}^2-cell quadratic-mapped grid",
+            "ms": [round(t * 1e3, 3) for t in ts], "points_per_s": round(px.numel() / min(ts), 0),
+            "outside": int((oi == np.iinfo(np.int64).max).sum().item()), "sample_equals_oracle": same}
 
 
 def run_differentiable(args, torch):
@@ -974,6 +1003,7 @@ LEGS = {
     "differentiable": lambda args, torch: run_differentiable(args, torch),
     "interp_2d": lambda args, torch: run_interp(args, torch),
     "fill": lambda args, torch: run_fill(args, torch),
+    "find_indices_2d": lambda args, torch: run_find_indices_2d(args, torch),
     "serving": lambda args, torch: run_serving(args, torch),
 }
 
@@ -999,7 +1029,9 @@ def main(argv=None):
     p.add_argument("--serve-switch-ms", type=float, default=0.0, help="GIL switch interval (0: unchanged)")
     p.add_argument("--no-extra", action="store_true", help="skip the differentiable-regrid and batched legs")
     p.add_argument("--only", choices=sorted(LEGS), help="run one secondary leg alone and print its JSON (profiling)")
-    p.add_argument("--small", action="store_true", help="with --only: the leg's reduced profiling size")
+    p.add_argument("--small", action="store_true",
+                   help="with --only: the leg's reduced profiling size (interp_2d, fill, multilinear_1d, "
+                        "conservative_1d, batched)")
     args = p.parse_args(argv)
     if args.warmup < 3:
         args.warmup = 3

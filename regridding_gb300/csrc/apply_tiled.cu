@@ -34,7 +34,7 @@ namespace {
 
 constexpr int WARPS = 8;        // warp tiles per block
 constexpr int TR = 4, TC = 8;   // warp tile: TR output rows x TC output columns
-constexpr int PREP_MAX = 4096;  // entries of one warp tile sorted in shared memory
+constexpr int PREP_MAX = 1024;  // entries of one warp tile sorted in shared memory (4 KB per warp)
 constexpr int CACHED_T = 8;     // row entries kept in registers across slices
 constexpr int SLICES = 4;       // stack slices staged per step
 
@@ -365,7 +365,7 @@ __device__ __forceinline__ int64_t patch_cell(const PatchGrid& P, int64_t p, int
 // gathers (origin row -2).
 template <int PASS>
 __global__ void __launch_bounds__(256)
-    prepare_patch(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, PatchGrid P, int64_t n1_in,
+    prepare_patch(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, PatchGrid P, FastDiv nd,
                   int2* __restrict__ origin, int2* __restrict__ extent, unsigned* __restrict__ stats, int BR,
                   uint16_t* __restrict__ slot) {
     __shared__ int red[4][8];
@@ -381,7 +381,7 @@ __global__ void __launch_bounds__(256)
         int rmin = INT_MAX, rmax = -1, cmin = INT_MAX, cmax = -1;
         for (int64_t k = s; k < e; k++) {
             const int c = col[k];
-            const int r = (int)(c / n1_in), cc = (int)(c - (int64_t)r * n1_in);
+            const int r = (int)nd.div((uint32_t)c), cc = c - r * (int)nd.d;
             rmin = min(rmin, r);
             rmax = max(rmax, r);
             cmin = min(cmin, cc);
@@ -431,15 +431,16 @@ __global__ void __launch_bounds__(256)
     }
     for (int64_t k = s; k < e; k++) {
         const int c = col[k];
-        const int r = (int)(c / n1_in) - org.x, cc = (int)(c - (int64_t)(c / n1_in) * n1_in) - org.y;
+        const int row = (int)nd.div((uint32_t)c);
+        const int r = row - org.x, cc = c - row * (int)nd.d - org.y;
         slot[k] = (uint16_t)(r * PBOX_C + ((((cc >> 2) ^ (r & 7)) << 2) | (cc & 3)));
     }
 }
 
 // Box slot of input cell c (the slot prepare_patch gives it).
-__device__ __forceinline__ int box_slot_of(int c, int2 org, int64_t n1_in) {
-    const int row = (int)(c / n1_in);
-    const int r = row - org.x, cc = (int)(c - (int64_t)row * n1_in) - org.y;
+__device__ __forceinline__ int box_slot_of(int c, int2 org, FastDiv nd) {
+    const int row = (int)nd.div((uint32_t)c);
+    const int r = row - org.x, cc = c - row * (int)nd.d - org.y;
     return r * PBOX_C + ((((cc >> 2) ^ (r & 7)) << 2) | (cc & 3));
 }
 
@@ -457,12 +458,15 @@ __device__ __forceinline__ float weight_rest(double w, float hi) {
 // reading the same word share one access.  One block per patch, its threads
 // laid out as in the apply kernel that will read the order (perm null: the
 // warp tiles of the fast kernel; else thread t takes patch cell perm[t], the
-// row-length order of the compensated kernel): for every step, lane by lane,
-// each lane takes a remaining entry whose word an earlier lane reads at this
-// step, else one whose bank no earlier lane uses, else its first remaining
-// entry.  (Neighbouring output cells share input cells, so shared words are
-// common: on the 1024^2 -> 768^2 weights this takes the warp tiles' gathers
-// from 1.81 to 1.56 accesses per step.)  The entries' natural slots come from
+// row-length order of the compensated kernel).  Greedy, step by step and
+// lane by lane in lane order: each lane takes the first of its remaining
+// entries whose word an earlier lane reads at this step, else the first
+// whose bank no earlier lane uses, else its first remaining entry.
+// (Neighbouring output cells share input cells, so shared words are common:
+// on the 1024^2 -> 768^2 weights this takes the warp tiles' gathers from
+// 1.81 to 1.56 accesses per step.)  A lane's turn is taken by the whole
+// warp: lane c tests the lane's candidate c against the step's bank owners
+// and two ballots give the pick.  The entries' natural slots come from
 // slot_in, or from their columns when it is null; writes the reordered
 // slots, float32 weights and (lo_out non-null) the weights' float32 rests.
 // The CSR itself, which fixes the exact paths' order, is unchanged.  Lanes
@@ -470,10 +474,12 @@ __device__ __forceinline__ float weight_rest(double w, float hi) {
 constexpr int ORDER_MAX = 16;
 
 __global__ void __launch_bounds__(32 * PATCH_WARPS)
-    order_patch(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, int64_t n1_in,
+    order_patch(const int64_t* __restrict__ row_ptr, const int32_t* __restrict__ col, FastDiv nd,
                 const float* __restrict__ val32, const double* __restrict__ val, PatchGrid P,
                 const int2* __restrict__ origin, const uint8_t* __restrict__ perm, const uint16_t* slot_in,
                 uint16_t* slot_out, float* __restrict__ hi_out, float* __restrict__ lo_out) {
+    __shared__ uint16_t cand[PATCH_WARPS][32][ORDER_MAX];  // every lane's natural slots
+    __shared__ uint16_t owner[PATCH_WARPS][32];            // the word each bank serves at this step
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
     int pr = 4 * (warp >> 1) + (lane >> 3), pc = 8 * (warp & 1) + (lane & 7);
@@ -492,7 +498,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
     const int2 org = origin[p];
     if (org.x < 0) return;  // block-uniform
     auto natural = [&](int64_t k) -> uint16_t {
-        return slot_in ? slot_in[k] : (uint16_t)box_slot_of(col[k], org, n1_in);
+        return slot_in ? slot_in[k] : (uint16_t)box_slot_of(col[k], org, nd);
     };
     if (nk > ORDER_MAX) {
         for (int64_t k = s; k < e; k++) {
@@ -502,44 +508,37 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
         }
         // keep the stored order, but the other lanes still take part below
     }
-    uint16_t sl[ORDER_MAX];
-    float vl[ORDER_MAX], vr[ORDER_MAX];
     const int mine = nk <= ORDER_MAX ? nk : 0;
-    for (int k = 0; k < ORDER_MAX; k++) {
-        sl[k] = k < mine ? natural(s + k) : 0;
-        vl[k] = k < mine ? val32[s + k] : 0.f;
-        vr[k] = (k < mine && lo_out) ? weight_rest(val[s + k], vl[k]) : 0.f;
-    }
-    unsigned left = mine == 32 ? 0xffffffffu : ((1u << mine) - 1u);  // entries not yet placed
-    int kmax = mine;
-    for (int off = 16; off > 0; off >>= 1) kmax = max(kmax, __shfl_xor_sync(0xffffffffu, kmax, off));
-    // the word each bank serves at this step (0xffff: none yet), per warp
-    __shared__ uint16_t owner[PATCH_WARPS][32];
+    for (int c = 0; c < mine; c++) cand[warp][lane][c] = natural(s + c);
+    unsigned left = mine ? ((1u << mine) - 1u) : 0u;  // entries not yet placed (mine <= 16)
+    const int kmax = __reduce_max_sync(0xffffffffu, mine);
+    __syncwarp();
+    const int c = lane & (ORDER_MAX - 1);  // the candidate this lane tests at each turn
     for (int k = 0; k < kmax; k++) {
         owner[warp][lane] = 0xffffu;
         __syncwarp();
         for (int l = 0; l < 32; l++) {
-            if (lane == l && left) {
-                int pick = -1;
-                for (int c = 0; c < ORDER_MAX; c++)  // a word an earlier lane reads at this step
-                    if (pick < 0 && ((left >> c) & 1) && owner[warp][sl[c] & 31] == sl[c]) pick = c;
-                for (int c = 0; c < ORDER_MAX; c++)  // else a bank no earlier lane uses
-                    if (pick < 0 && ((left >> c) & 1) && owner[warp][sl[c] & 31] == 0xffffu) pick = c;
-                if (pick < 0) pick = __ffs(left) - 1;
+            const unsigned lleft = __shfl_sync(0xffffffffu, left, l);
+            if (lleft == 0u) continue;  // warp-uniform
+            bool share = false, freeb = false;
+            if (lane < ORDER_MAX && ((lleft >> c) & 1u)) {
+                const uint16_t w = cand[warp][l][c];
+                const uint16_t ow = owner[warp][w & 31];
+                share = ow == w;
+                freeb = ow == 0xffffu;
+            }
+            const unsigned ms = __ballot_sync(0xffffffffu, share), mf = __ballot_sync(0xffffffffu, freeb);
+            const int pick = ms ? __ffs(ms) - 1 : (mf ? __ffs(mf) - 1 : __ffs(lleft) - 1);
+            if (lane == l) {
                 left &= ~(1u << pick);
-                // place entry `pick` at position k: registers are indexed by
-                // loop counters only, so write it out directly
-                for (int c = 0; c < ORDER_MAX; c++)
-                    if (c == pick) {
-                        if (owner[warp][sl[c] & 31] == 0xffffu) owner[warp][sl[c] & 31] = sl[c];
-                        slot_out[s + k] = sl[c];
-                        hi_out[s + k] = vl[c];
-                        if (lo_out) lo_out[s + k] = vr[c];
-                    }
+                const uint16_t w = cand[warp][l][pick];
+                if (owner[warp][w & 31] == 0xffffu) owner[warp][w & 31] = w;
+                slot_out[s + k] = w;
+                hi_out[s + k] = val32[s + pick];
+                if (lo_out) lo_out[s + k] = weight_rest(val[s + pick], val32[s + pick]);
             }
             __syncwarp();
         }
-        __syncwarp();
     }
 }
 
@@ -644,7 +643,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     apply_patch_tma(const __grid_constant__ CUtensorMap tmap, const int64_t* __restrict__ row_ptr,
                     const int32_t* __restrict__ col, const uint16_t* __restrict__ slot,
                     const float* __restrict__ bval, const float* __restrict__ blo, const float* __restrict__ val,
-                    const double* __restrict__ dval, double* __restrict__ vout64, int64_t n1_in,
+                    const double* __restrict__ dval, double* __restrict__ vout64, FastDiv nd,
                     PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
                     unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
                     int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags,
@@ -703,7 +702,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
 #pragma unroll
     for (int k = 0; k < CT; k++) {
         if constexpr (EXACT) {
-            li[k] = k < nk ? box_slot_of(col[s + k], org, n1_in) : 0;
+            li[k] = k < nk ? box_slot_of(col[s + k], org, nd) : 0;
             wd[k] = k < nk ? dval[s + k] : 0.0;
             w[k] = 0.f;
             wl[k] = 0.f;
@@ -758,7 +757,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                 }
                 for (int64_t k = s + CT; k < e; k++) {
                     const double wk = dval[k];
-                    const int sk = box_slot_of(col[k], org, n1_in);
+                    const int sk = box_slot_of(col[k], org, nd);
 #pragma unroll
                     for (int q = 0; q < SPS; q++)
                         acc[q] = __dadd_rn(acc[q], __dmul_rn(wk, widen(buf[q * plane + (sk ^ ((q & 1) ? flip : 0))])));
@@ -804,7 +803,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                         // float64, stored order (the exact apply's sum)
                         r = 0.0;
                         for (int64_t k = s; k < e; k++)
-                            r = __dadd_rn(r, __dmul_rn(dval[k], widen(buf[q * plane + (box_slot_of(col[k], org, n1_in) ^
+                            r = __dadd_rn(r, __dmul_rn(dval[k], widen(buf[q * plane + (box_slot_of(col[k], org, nd) ^
                                                                                      ((q & 1) ? flip : 0))])));
                     }
                     vout64[(ds + q) * n_out + o] = r;
@@ -1245,7 +1244,7 @@ int ff_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         if ((st = dalloc(&W->ff_hi, (size_t)W->nnz, s))) break;
         if ((st = dalloc(&W->ff_lo, (size_t)W->nnz, s))) break;
         order_patch<<<(unsigned)W->box_patches, 32 * PATCH_WARPS, 0, s>>>(
-            W->row_ptr, W->col, W->in_shape1, W->val32, W->val, patch_grid(W), W->box_origin, W->box_perm, nullptr,
+            W->row_ptr, W->col, FastDiv((uint32_t)W->in_shape1), W->val32, W->val, patch_grid(W), W->box_origin, W->box_perm, nullptr,
             W->ff_slot, W->ff_hi, W->ff_lo);
         if (cudaGetLastError() != cudaSuccess) {
             set_error("apply (compensated lists): launch failed");
@@ -1282,7 +1281,7 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
             cudaMemsetAsync(W->dflags, 0, sizeof(unsigned), s);
         }
         cudaMemsetAsync(stats, 0, 4 * sizeof(unsigned), s);
-        prepare_patch<0><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, W->in_shape1, W->box_origin,
+        prepare_patch<0><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, FastDiv((uint32_t)W->in_shape1), W->box_origin,
                                                            extent, stats, 0, nullptr);
         unsigned h[4] = {0, 0, 0, 0};
         small_to_host(h, stats, sizeof(h), s);
@@ -1294,7 +1293,7 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         }
         // box rows: a multiple of 4 (keeps the swizzle phase of every slice at 0 or 4)
         const int BR = (int)((std::min<unsigned>(std::max<unsigned>(h[0], 1u), PBOX_MAX_R) + 3) & ~3u);
-        prepare_patch<1><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, W->in_shape1, W->box_origin,
+        prepare_patch<1><<<(unsigned)patches, 256, 0, s>>>(W->row_ptr, W->col, P, FastDiv((uint32_t)W->in_shape1), W->box_origin,
                                                            extent, stats, BR, W->box_slot);
         small_to_host(h, stats, sizeof(h), s);
         e = cudaStreamSynchronize(s);
@@ -1306,12 +1305,13 @@ int box_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         W->box_rows = BR;
         W->box_cols = PBOX_C;
         W->box_patches = patches;
-        if ((st = dalloc(&W->box_val, (size_t)W->nnz, s))) break;
-        order_patch<<<(unsigned)patches, 32 * PATCH_WARPS, 0, s>>>(W->row_ptr, W->col, W->in_shape1, W->val32,
-                                                                   W->val, P, W->box_origin, nullptr, W->box_slot,
-                                                                   W->box_slot, W->box_val, nullptr);
         const bool few = (int64_t)h[2] * 100 <= patches || h[2] <= 4;  // patches left to direct gathers
         W->box_state = few && BR <= W->in_shape0 && PBOX_C <= W->in_shape1 ? 1 : -1;
+        if (W->box_state != 1) break;  // footprints too large for a box: no entry order needed
+        if ((st = dalloc(&W->box_val, (size_t)W->nnz, s))) break;
+        order_patch<<<(unsigned)patches, 32 * PATCH_WARPS, 0, s>>>(W->row_ptr, W->col, FastDiv((uint32_t)W->in_shape1),
+                                                                   W->val32, W->val, P, W->box_origin, nullptr,
+                                                                   W->box_slot, W->box_slot, W->box_val, nullptr);
     } while (0);
     dfree(extent, s);
     dfree(stats, s);
@@ -1375,7 +1375,7 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     constexpr bool FF = MODE == MODE_FF;
     apply_patch_tma<SPS, NST, MINB, MODE, CT><<<grid, 32 * PATCH_WARPS, smem, s>>>(
         map, W->row_ptr, W->col, FF ? W->ff_slot : W->box_slot, FF ? W->ff_hi : W->box_val, FF ? W->ff_lo : nullptr,
-        W->val32, W->val, OUT64 ? (double*)vout : nullptr, W->in_shape1, patch_grid(W), patches, W->box_origin, BR,
+        W->val32, W->val, OUT64 ? (double*)vout : nullptr, FastDiv((uint32_t)W->in_shape1), patch_grid(W), patches, W->box_origin, BR,
         stage_floats, stage_bytes, vin, W->n_in, OUT64 ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags,
         OUT64 ? W->box_perm : nullptr);
     RG_CUDA(cudaGetLastError());

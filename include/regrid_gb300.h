@@ -226,6 +226,13 @@ int rg_locate_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, c
  * At most RG_LOCATE_NOALLOC_MAX_POINTS points per call (RG_ERR_ARG beyond).
  * Every call on a device shares the one array, so calls that overlap on the
  * GPU (different streams, or host threads) race and must be serialised.
+ * The looked-up address is kept until the process exits: resetting a device
+ * (cudaDeviceReset) after the first call on it is not supported.
+ * Points the walk cannot place (every point outside the grid) go to a
+ * fallback that scans all 2 (nx + ny - 2) boundary edges with one warp per
+ * point, about (nx + ny) / 16 edge tests per lane: with many points outside
+ * a large grid this costs far more than rg_locate_2d, whose fallback bins
+ * the boundary edges by y.
  * Results equal rg_locate_2d with method 2. */
 int rg_locate_2d_noalloc(const double* d_x, const double* d_y, int64_t nx, int64_t ny,
                          const double* d_px, const double* d_py, int64_t npts, int64_t* d_i,

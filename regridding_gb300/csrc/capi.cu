@@ -310,7 +310,7 @@ using namespace rg;
 
 extern "C" {
 
-int rg_version(void) { return 100; }
+int rg_version(void) { return 200; }
 
 int rg_copy_from_host(void* d_dst, const void* h_src, int64_t nbytes, rg_stream_t stream) {
     RG_CHECK(nbytes >= 0 && (nbytes == 0 || (d_dst && h_src)), RG_ERR_ARG, "rg_copy_from_host: bad arguments");

@@ -434,7 +434,8 @@ void* g_scratch_address[256] = {};  // per device ordinal, filled on first use
 
 // Device address of g_locate_scratch on the current device.  In host code the
 // array's name only stands in for the symbol, so the address is looked up
-// once per device, with that device current.
+// once per device, with that device current, and kept until the process
+// exits (a device reset after the first call is not supported).
 int scratch_address(void** out) {
     int dev = 0;
     RG_CUDA(cudaGetDevice(&dev));

@@ -21,7 +21,10 @@ caller.  This module gives that form a file:
 * :class:`WeightsDiskCache` — a directory of such files named by the hash of
   everything the weights depend on (coordinate arrays, axes,
   ``weights_input``, method, bounds, perturbation and seed; the coordinate
-  hashes are the serving cache's :func:`~regridding_gb300.serving.grid_key`).
+  hashes are the serving cache's :func:`~regridding_gb300.serving.grid_key`)
+  and of the build that makes them (:func:`build_tag`: library version and
+  weights revision, also stored in every file's header and checked on a
+  hit).  A short or corrupt file reads as a miss.
   :meth:`WeightsDiskCache.weights` has the signature of
   :func:`regridding_gb300.weights` and returns the stored layout on a hit,
   else builds, stores and returns it.  Files are written to a temporary name
@@ -48,6 +51,18 @@ __all__ = ["save_weights", "load_weights", "WeightsDiskCache", "weights_key"]
 MAGIC = b"RGWEIGHTS1\0\0\0\0\0\0"
 PREAMBLE = 64
 ALIGN = 4096
+WEIGHTS_REVISION = 2
+"""Raised whenever the weights this library builds from the same arguments
+may change (an arithmetic or layout change of the build); with the
+library version it names the build that wrote a cache file."""
+
+
+def build_tag() -> str:
+    """The library version and weights revision: part of every cache key and
+    of every file's header, so a cache never serves weights of another build."""
+    from . import _lib
+
+    return f"rg{int(_lib.load().rg_version())}-w{WEIGHTS_REVISION}"
 
 
 def _align(n: int) -> int:
@@ -85,6 +100,7 @@ def save_weights(path, weights, meta: dict | None = None) -> int:
         "shape_input": [int(s) for s in shape_input],
         "shape_output": [int(s) for s in shape_output],
         "entries": total,
+        "build": build_tag(),
         "meta": meta or {},
     }
     # layout: preamble | header | offsets | indices_input | indices_output | values
@@ -138,9 +154,16 @@ def load_weights(path, mmap: bool = True):
     memory mapping of the file; otherwise they are read into memory (and
     are still read-only)."""
     header = read_header(path)
-    total = int(header["entries"])
-    n_elem = int(np.prod(header["shape"], dtype=np.int64))
-    s_off, s_in, s_out, s_val = header["offsets"]
+    try:
+        total = int(header["entries"])
+        n_elem = int(np.prod(header["shape"], dtype=np.int64))
+        s_off, s_in, s_out, s_val = (int(v) for v in header["offsets"])
+    except (KeyError, TypeError, ValueError) as exc:
+        raise ValueError(f"{path}: malformed header ({exc})") from None
+    size = os.path.getsize(path)
+    ends = (s_off + 8 * (n_elem + 1), s_in + 8 * total, s_out + 8 * total, s_val + 8 * total)
+    if total < 0 or n_elem < 0 or min(s_off, s_in, s_out, s_val) < PREAMBLE or max(ends) > size:
+        raise ValueError(f"{path}: truncated or corrupt (arrays end past the file's {size} bytes)")
     if mmap:
         mm = np.memmap(path, dtype=np.uint8, mode="r")
 
@@ -154,6 +177,8 @@ def load_weights(path, mmap: bool = True):
             return blob[start: start + count * 8].view(dtype)
 
     offsets = view(s_off, n_elem + 1, np.int64)
+    if offsets[0] != 0 or offsets[-1] != total or np.any(np.diff(offsets) < 0):
+        raise ValueError(f"{path}: corrupt element offsets")
     ii, oo, vv = view(s_in, total, np.int64), view(s_out, total, np.int64), view(s_val, total, np.float64)
     flat = np.empty(n_elem, dtype=object)
     for k in range(n_elem):
@@ -202,6 +227,7 @@ def weights_key(coordinates_input, coordinates_output, axis_input=None, axis_out
         "bounds": bounds if method == "multilinear" else None,
         "perturb": bool(perturb),
         "seed": None if (seed is None or not perturb) else int(seed),
+        "build": build_tag(),
     }
     return hashlib.sha256(json.dumps(parts, sort_keys=True).encode()).hexdigest()[:40]
 
@@ -227,8 +253,10 @@ class WeightsDiskCache:
             return None
         p = self.path(key)
         try:
+            if read_header(p).get("build") != build_tag():
+                raise ValueError("written by another build")
             w = load_weights(p, mmap=mmap)
-        except (FileNotFoundError, ValueError):
+        except (FileNotFoundError, ValueError, json.JSONDecodeError):
             with self._lock:
                 self.misses += 1
             return None

@@ -68,6 +68,52 @@ def test_not_a_weights_file(tmp_path):
         store.load_weights(p)
 
 
+def test_truncated_or_corrupt_files_are_rejected(tmp_path):
+    """A short file, element offsets that do not add up, and a header whose
+    arrays lie past the end raise ValueError (which the cache treats as a
+    miss), instead of returning silently truncated elements."""
+    from regridding_gb300 import store
+
+    rng = np.random.default_rng(3)
+    w = layout(rng, (5,))
+    p = tmp_path / "w.rgw"
+    store.save_weights(p, w)
+    full = p.read_bytes()
+    header = store.read_header(p)
+    short = tmp_path / "short.rgw"
+    short.write_bytes(full[: header["offsets"][3] + 8])  # values cut off
+    with pytest.raises(ValueError, match="truncated"):
+        store.load_weights(short)
+    bad = bytearray(full)
+    s_off = header["offsets"][0]
+    bad[s_off + 8: s_off + 16] = (10**6).to_bytes(8, "little")  # the second element's end offset
+    corrupt = tmp_path / "corrupt.rgw"
+    corrupt.write_bytes(bytes(bad))
+    with pytest.raises(ValueError, match="offsets"):
+        store.load_weights(corrupt)
+    cache = store.WeightsDiskCache(tmp_path / "c")
+    os.replace(short, cache.path("k1"))
+    assert cache.get("k1") is None and cache.misses == 1
+
+
+def test_cache_ignores_files_of_another_build(tmp_path, monkeypatch):
+    """Keys and file headers carry the library version and weights revision:
+    a file written by another build is a miss, never a hit."""
+    from regridding_gb300 import store
+
+    rng = np.random.default_rng(4)
+    cache = store.WeightsDiskCache(tmp_path)
+    cache.put("k", layout(rng, (2,)))
+    assert cache.get("k") is not None
+    assert store.read_header(cache.path("k"))["build"] == store.build_tag()
+    monkeypatch.setattr(store, "WEIGHTS_REVISION", store.WEIGHTS_REVISION + 1)
+    assert cache.get("k") is None
+    gi = (np.linspace(0, 1, 5),)
+    k2 = store.weights_key(gi, gi)
+    monkeypatch.setattr(store, "WEIGHTS_REVISION", store.WEIGHTS_REVISION + 1)
+    assert store.weights_key(gi, gi) != k2
+
+
 def test_key_rules():
     from regridding_gb300 import store
 

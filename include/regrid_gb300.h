@@ -51,8 +51,10 @@ typedef struct CUstream_st* rg_stream_t; /* == cudaStream_t */
 /* float32 input, float64 output: every product and partial sum carried as an
  * unevaluated pair of floats (error-free products by FMA, Knuth's two-sum) on
  * the FP32 pipe, the pair added in double at the end.  Result within
- * (1.1e-14 + n^2 * 3.6e-15) * sum_k |w_k x_k| of the exact sum for rows of n
- * entries (checked to 1e-12 relative against the upstream float64 apply).
+ * (1.1e-14 + (n + 2)^2 * 3.6e-15) * sum_k |w_k x_k| of the exact sum for rows
+ * of n entries (checked to 1e-12 relative against the upstream float64 apply).
+ * A float32 partial sum that overflows, or a non-finite input or weight,
+ * sends that output and slice to the exact float64 sum instead.
  * Every other dtype combination computes as RG_ACC_EXACT. */
 #define RG_ACC_COMPENSATED 2
 
@@ -162,7 +164,9 @@ int rg_weights_free(rg_weights w, rg_stream_t stream);
  * (stack, n_out) of dtype_out.  acc = RG_ACC_EXACT reproduces the upstream
  * float64 result bit for bit (dtype_out must be RG_F64, or RG_F32 for the
  * upstream in-place float32 output, which rounds after every update);
- * RG_ACC_FAST accumulates in dtype_out with FMA. */
+ * RG_ACC_FAST accumulates in dtype_out with FMA; RG_ACC_COMPENSATED gives a
+ * float64 result within 1e-12 of the upstream's for float32 input at
+ * close to the FAST path's speed (see its definition above). */
 int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dtype_out,
              int64_t stack, int acc, rg_stream_t stream);
 

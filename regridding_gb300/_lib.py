@@ -78,20 +78,27 @@ class RegridError(RuntimeError):
     """A failure reported by the CUDA library."""
 
 
+def debug_requested() -> bool:
+    """RG_DEBUG=1 selects the bounds-checked debug library."""
+    return os.environ.get("RG_DEBUG", "") not in ("", "0")
+
+
 def library_path() -> str:
-    return _build.LIB
+    return _build.LIB_DEBUG if debug_requested() else _build.LIB
 
 
 def load(build_if_missing: bool = True) -> ctypes.CDLL:
-    """Load (building first if needed) the CUDA library."""
+    """Load (building first if needed) the CUDA library: the release build,
+    or with RG_DEBUG=1 the bounds-checked debug build."""
     global _lib
     with _lock:
         if _lib is None:
-            path = _build.LIB
+            debug = debug_requested()
+            path = library_path()
             if not os.path.exists(path):
                 if not build_if_missing:
-                    raise RegridError(f"{path} is missing; run regridding_gb300._build.build()")
-                _build.build()
+                    raise RegridError(f"{path} is missing; run regridding_gb300._build.build(debug={debug})")
+                _build.build(debug=debug)
             lib = ctypes.CDLL(path)
             for name, args in SIGNATURES.items():
                 fn = getattr(lib, name)

@@ -251,6 +251,7 @@ extern "C" int rg_conservative_2d_grad_output(rg_weights w, const double* d_xi, 
                                               int64_t nyo, const double* d_w_in, const void* d_values,
                                               const void* d_grad_out, int dtype, int64_t stack, double* d_grad_xo,
                                               double* d_grad_yo, double* d_w_check, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_conservative_2d_grad_output");
     using namespace rg;
     RG_CHECK(w, RG_ERR_ARG, "rg_conservative_2d_grad_output: NULL handle");
     RG_CHECK(nxi >= 2 && nyi >= 2 && nxo >= 2 && nyo >= 2, RG_ERR_ARG,

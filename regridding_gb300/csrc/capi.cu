@@ -347,6 +347,7 @@ int rg_last_error(char* buf, size_t n) {
 int rg_build_conservative_2d(const double* d_xi, const double* d_yi, int64_t nxi, int64_t nyi,
                              const double* d_xo, const double* d_yo, int64_t nxo, int64_t nyo,
                              const double* d_w_in, rg_stream_t stream, rg_weights* out) {
+    rg::NvtxRange nvtx_range("rg_build_conservative_2d");
     RG_CHECK(out, RG_ERR_ARG, "rg_build_conservative_2d: out is NULL");
     *out = nullptr;
     rg_weights_s* W = new (std::nothrow) rg_weights_s();
@@ -367,6 +368,7 @@ int rg_build_conservative_2d_batch(int64_t n, const double* const* d_xi, const d
                                    const double* const* d_yo, const int64_t* nxo, const int64_t* nyo,
                                    const double* const* d_w_in, rg_stream_t stream, rg_weights* out,
                                    int* status) {
+    rg::NvtxRange nvtx_range("rg_build_conservative_2d_batch");
     RG_CHECK(n >= 1 && n < (1 << 24), RG_ERR_ARG, "rg_build_conservative_2d_batch: bad pair count %lld",
              (long long)n);
     RG_CHECK(d_xi && d_yi && nxi && nyi && d_xo && d_yo && nxo && nyo && out && status, RG_ERR_ARG,
@@ -404,6 +406,7 @@ int rg_build_conservative_2d_batch(int64_t n, const double* const* d_xi, const d
 
 int rg_weights_from_coo(const int64_t* d_in, const int64_t* d_out, const double* d_val, int64_t nnz,
                         int64_t n_in, int64_t n_out, rg_stream_t stream, rg_weights* out) {
+    rg::NvtxRange nvtx_range("rg_weights_from_coo");
     RG_CHECK(out, RG_ERR_ARG, "rg_weights_from_coo: out is NULL");
     RG_CHECK(nnz >= 0 && n_in >= 0 && n_out >= 0, RG_ERR_ARG, "rg_weights_from_coo: negative size");
     RG_CHECK(n_in < INT32_MAX && n_out < INT32_MAX, RG_ERR_UNSUPPORTED,
@@ -489,6 +492,7 @@ int rg_weights_set_output_shape(rg_weights w, int64_t n0, int64_t n1) {
 
 int rg_weights_export_coo(rg_weights w, int64_t* d_in, int64_t* d_out, double* d_val,
                           rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_weights_export_coo");
     RG_CHECK(w, RG_ERR_ARG, "rg_weights_export_coo: NULL handle");
     if (w->nnz == 0) return RG_OK;
     cudaStream_t s = (cudaStream_t)stream;
@@ -539,18 +543,21 @@ int rg_weights_free(rg_weights w, rg_stream_t stream) {
 
 int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dtype_out, int64_t stack,
              int acc, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_apply");
     RG_CHECK(w, RG_ERR_ARG, "rg_apply: NULL handle");
     return apply_weights(w, false, d_vin, dtype_in, d_vout, dtype_out, stack, acc, (cudaStream_t)stream);
 }
 
 int rg_apply_host(rg_weights w, const void* h_vin, int dtype_in, void* h_vout, int dtype_out, int64_t stack,
                   int acc, int64_t chunk, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_apply_host");
     RG_CHECK(w, RG_ERR_ARG, "rg_apply_host: NULL handle");
     return apply_host(w, h_vin, dtype_in, h_vout, dtype_out, stack, acc, chunk, (cudaStream_t)stream);
 }
 
 int rg_apply_transpose(rg_weights w, const void* d_vout, int dtype_out, void* d_vin, int dtype_in,
                        int64_t stack, int acc, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_apply_transpose");
     RG_CHECK(w, RG_ERR_ARG, "rg_apply_transpose: NULL handle");
     return apply_weights(w, true, d_vout, dtype_out, d_vin, dtype_in, stack, acc, (cudaStream_t)stream);
 }
@@ -569,6 +576,7 @@ int rg_cell_length_1d(const double* d_x, int64_t nd, int64_t n, double* d_len, r
 int rg_locate_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, const double* d_px,
                  const double* d_py, int64_t npts, int method, int64_t* d_i, int64_t* d_j,
                  rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_locate_2d");
     RG_CHECK(nx >= 2 && ny >= 2, RG_ERR_ARG, "rg_locate_2d: need at least 2x2 vertices");
     RG_CHECK(method >= 0 && method <= 2, RG_ERR_ARG, "rg_locate_2d: unknown method %d", method);
     if (method == 2)
@@ -579,6 +587,7 @@ int rg_locate_2d(const double* d_x, const double* d_y, int64_t nx, int64_t ny, c
 int rg_find_indices_1d(const double* d_xin, int64_t in_stride, int64_t m, const double* d_xout,
                        int64_t out_stride, int64_t n, int64_t nd, int method, int64_t fill_value,
                        int64_t* d_result, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_find_indices_1d");
     return find_indices_1d(d_xin, in_stride, m, d_xout, out_stride, n, nd, method, fill_value, d_result,
                            (cudaStream_t)stream);
 }
@@ -587,6 +596,7 @@ int rg_multilinear_1d(const double* d_xin, int64_t in_stride, int64_t m, const d
                       const double* d_xout_search, int64_t out_stride, int64_t n, int64_t nd,
                       const double* d_w_in, int64_t w_stride, int bounds, int64_t* d_ind_in,
                       int64_t* d_ind_out, double* d_val, int64_t* h_n_outside, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_multilinear_1d");
     return multilinear_1d(d_xin, in_stride, m, d_xout, d_xout_search, out_stride, n, nd, d_w_in, w_stride,
                           bounds, d_ind_in, d_ind_out, d_val, h_n_outside, (cudaStream_t)stream);
 }
@@ -595,6 +605,7 @@ int rg_conservative_1d(const double* d_xin, int64_t in_stride, int64_t m, const 
                        int64_t out_stride, int64_t n, int64_t nd, const double* d_w_in, int64_t w_stride,
                        int64_t cap, int64_t* d_ind_in, int64_t* d_ind_out, double* d_val, int64_t* d_count,
                        rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_conservative_1d");
     return conservative_1d(d_xin, in_stride, m, d_xout, out_stride, n, nd, d_w_in, w_stride, cap, d_ind_in,
                            d_ind_out, d_val, d_count, (cudaStream_t)stream);
 }
@@ -603,6 +614,7 @@ int rg_transpose_conservative_scale(const int64_t* d_in, const int64_t* d_out, c
                                     int64_t nnz, const double* d_vol_in, int64_t n_in,
                                     const double* d_vol_out, int64_t n_out, const double* d_w_in,
                                     double* d_result, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_transpose_conservative_scale");
     return transpose_conservative_scale(d_in, d_out, d_val, nnz, d_vol_in, n_in, d_vol_out, n_out, d_w_in,
                                         d_result, (cudaStream_t)stream);
 }

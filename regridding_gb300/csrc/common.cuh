@@ -8,9 +8,21 @@
 #include <mutex>
 #include <string>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "../../include/regrid_gb300.h"
 
 namespace rg {
+
+// A named NVTX range over the extent of a C entry point, shown by the Nsight
+// tools on the host timeline (without a tool attached a push or pop is a
+// check of an unset function pointer).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
 
 // ---------------------------------------------------------------------------
 // error reporting: every C entry point returns an RG_* status and records a
@@ -53,6 +65,7 @@ enum DeviceFlag : unsigned {
     FLAG_BUCKET_TOO_LONG = 1u << 2,
     FLAG_CAPACITY = 1u << 3,
     FLAG_TIMEOUT = 1u << 4,  // a bounded wait for an asynchronous copy gave up
+    FLAG_BOUNDS = 1u << 5,   // (debug builds, -DRG_DEBUG) a grid read outside its array
 };
 
 // ---------------------------------------------------------------------------

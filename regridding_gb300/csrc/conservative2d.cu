@@ -158,12 +158,29 @@ __device__ __forceinline__ double winding_term(double x, double y, double vx0, d
     return 0.0;
 }
 
+#ifdef RG_DEBUG
+// Debug builds (-DRG_DEBUG, regridding_gb300._build.build(debug=True)): every
+// grid read of the build is bounds-checked.  A read outside the array sets
+// FLAG_BOUNDS here and yields NaN (no trap: the build runs to its end and
+// the host turns the flag into RG_ERR_WALK).
+__device__ unsigned g_debug_flags;
+__device__ __forceinline__ bool debug_in_grid(int64_t i, int64_t j, int64_t nx, int64_t ny) {
+    if (i >= 0 && j >= 0 && i < nx && j < ny) return true;
+    atomicOr(&g_debug_flags, FLAG_BOUNDS);
+    return false;
+}
+#define RG_GRID_READ(a, i, j) \
+    (debug_in_grid(i, j, nx, ny) ? __ldg((a) + (i) * ny + (j)) : __longlong_as_double(0x7ff8000000000000ll))
+#else
+#define RG_GRID_READ(a, i, j) __ldg((a) + (i) * ny + (j))
+#endif
+
 struct Grid {
     const double* x;
     const double* y;
     int64_t nx, ny;
-    __device__ __forceinline__ double X(int64_t i, int64_t j) const { return __ldg(x + i * ny + j); }
-    __device__ __forceinline__ double Y(int64_t i, int64_t j) const { return __ldg(y + i * ny + j); }
+    __device__ __forceinline__ double X(int64_t i, int64_t j) const { return RG_GRID_READ(x, i, j); }
+    __device__ __forceinline__ double Y(int64_t i, int64_t j) const { return RG_GRID_READ(y, i, j); }
 };
 
 // point_is_inside_polygon on the 4 vertices of cell (i, j) in the order
@@ -1350,6 +1367,11 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
     }
     *nraw_out = -1;
     if (ch <= 0) return RG_OK;
+    // fault injection for tests: RG_FAULT_CHUNK_SLOTS caps the triple slots
+    // a chunk gets, so chunks overflow and the build takes its recovery path
+    // (whole-line walks, which count exactly); the weights do not change
+    int64_t slot_cap = INT64_MAX;
+    if (const char* env = getenv("RG_FAULT_CHUNK_SLOTS")) slot_cap = std::max<int64_t>(1, atoll(env));
     std::vector<ChunkPlan> C((size_t)G);
     std::vector<int64_t> chunk_base((size_t)G + 1, 0);
     int64_t chunks = 0, slots = 0;
@@ -1370,7 +1392,7 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
             if (!(cross < 1e6)) cross = 1e6;
             c.nc[f] = (F.len - 1 + ch - 1) / ch;
             c.chunk_base[f] = chunks;
-            c.cap[f] = 2 * ch * (1 + (int64_t)cross) + 32;
+            c.cap[f] = std::min<int64_t>(2 * ch * (1 + (int64_t)cross) + 32, slot_cap);
             c.slot_base[f] = slots;
             chunks += F.lines * c.nc[f];
             slots += F.lines * c.nc[f] * c.cap[f];
@@ -1768,6 +1790,21 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
             st = RG_ERR_CUDA;
             break;
         }
+#ifdef RG_DEBUG
+        unsigned dbg = 0;
+        const unsigned zero = 0;
+        cudaMemcpyFromSymbolAsync(&dbg, g_debug_flags, sizeof(unsigned), 0, cudaMemcpyDeviceToHost, s);
+        cudaMemcpyToSymbolAsync(g_debug_flags, &zero, sizeof(unsigned), 0, cudaMemcpyHostToDevice, s);
+        if (cudaStreamSynchronize(s) != cudaSuccess) {
+            set_error("conservative build (debug flags): %s", cudaGetErrorString(cudaGetLastError()));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        if (dbg & FLAG_BOUNDS) {
+            set_error("conservative build: debug bounds check: a grid read fell outside its array");
+            for (int g = 0; g < G; g++) status[g] = RG_ERR_WALK;
+        }
+#endif
     } while (0);
 
     dfree(area_in, s);

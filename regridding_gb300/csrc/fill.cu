@@ -656,6 +656,7 @@ int gauss_seidel_impl(T* a, const uint8_t* where, int64_t nt, int64_t ny, int64_
 
 extern "C" int rg_fill_median(const void* d_a, int dtype, const uint8_t* d_where, int64_t nt, int64_t slice,
                               void* d_out, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_fill_median");
     using namespace rg;
     RG_CHECK(dtype == RG_F32 || dtype == RG_F64, RG_ERR_ARG, "rg_fill_median: dtype must be RG_F32 or RG_F64");
     RG_CHECK(nt >= 0 && slice >= 0, RG_ERR_ARG, "rg_fill_median: negative size");
@@ -668,6 +669,7 @@ extern "C" int rg_fill_median(const void* d_a, int dtype, const uint8_t* d_where
 
 extern "C" int rg_fill_gauss_seidel(void* d_a, int dtype, const uint8_t* d_where, int64_t nt, int64_t ny, int64_t nx,
                                     const void* d_guess, int guess_kind, int64_t iterations, rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_fill_gauss_seidel");
     using namespace rg;
     RG_CHECK(dtype == RG_F32 || dtype == RG_F64, RG_ERR_ARG,
              "rg_fill_gauss_seidel: dtype must be RG_F32 or RG_F64");

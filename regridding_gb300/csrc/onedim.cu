@@ -575,6 +575,7 @@ __global__ void interp_kernel(const double* __restrict__ a, int64_t a_stride, in
 extern "C" int rg_interp_linear(const double* d_a, int64_t a_stride, int64_t nx, int64_t ny, const double* d_x,
                                 const double* d_y, int64_t i_stride, int64_t m, int64_t n_orth, double* d_out,
                                 rg_stream_t stream) {
+    rg::NvtxRange nvtx_range("rg_interp_linear");
     using namespace rg;
     RG_CHECK(nx >= 2 && (ny == 0 || ny >= 2) && m >= 0 && n_orth >= 0 && a_stride >= 0 && i_stride >= 0, RG_ERR_ARG,
              "rg_interp_linear: every interpolated axis needs at least 2 samples");

@@ -333,7 +333,15 @@ class GpuBackend:
         # room for the float32 weights and tile lists the first apply makes
         return nbytes.value + dw.nnz * 6 + (dw.n_out // 32 + 1) * 16
 
+    def _range(self, name: str):
+        """An NVTX range on the host timeline (Nsight tools)."""
+        return self.torch.cuda.nvtx.range(name)
+
     def build(self, slot, req: _Request):
+        with self._range("serve.build"):
+            return self._build(slot, req)
+
+    def _build(self, slot, req: _Request):
         dkey = self.disk_key(req) if self.disk is not None else None
         if dkey is not None:
             stored = self.disk.get(dkey)
@@ -405,6 +413,10 @@ class GpuBackend:
         return out
 
     def run(self, slot, weights, requests: list, staged=None) -> None:
+        with self._range("serve.apply"):
+            self._run(slot, weights, requests, staged)
+
+    def _run(self, slot, weights, requests: list, staged=None) -> None:
         t = self.torch
         with t.cuda.stream(slot.stream):
             if staged is not None:
@@ -515,6 +527,7 @@ class RegridServer:
         self.n_batches = 0
         self.n_builds = 0
         self.n_done = 0
+        self.n_cancelled = 0
         self._workers = [threading.Thread(target=self._worker, args=(i,), daemon=True, name=f"regrid-slot-{i}")
                          for i in range(slots)]
         for w in self._workers:
@@ -602,6 +615,7 @@ class RegridServer:
     def stats(self) -> dict:
         with self._cv:
             return {"done": self.n_done, "batches": self.n_batches, "builds": self.n_builds,
+                    "cancelled": self.n_cancelled,
                     "cache_entries": len(self.cache), "cache_bytes": self.cache.used,
                     "cache_hits": self.cache.hits, "cache_misses": self.cache.misses,
                     "evictions": self.cache.evictions, "peak_bytes": self.peak_bytes, "budget": self.budget}
@@ -648,10 +662,20 @@ class RegridServer:
             self._cv.notify_all()
         return progressed
 
+    def _drop_cancelled(self) -> None:
+        """Forget waiting requests whose futures the client cancelled."""
+        n = sum(1 for r in self._pending if r.future.cancelled())
+        if n:
+            self._pending = collections.deque(r for r in self._pending if not r.future.cancelled())
+            self.n_cancelled += n
+
     def _next_job(self) -> _Job | None:
         """The oldest waiting request whose grid is not being built, with the
         other waiting requests of its grid, if its footprint fits; None when
-        the oldest admissible request must wait for memory."""
+        the oldest admissible request must wait for memory.  A request
+        cancelled by its client before admission is dropped; once admitted
+        it runs to the end (its future can no longer be cancelled)."""
+        self._drop_cancelled()
         for head in list(self._pending):
             if head.key in self._building:
                 continue  # its weights are on the way; later requests may go first
@@ -681,6 +705,14 @@ class RegridServer:
                     return None  # wait for running jobs to free memory (no skipping ahead)
             for r in group:
                 self._pending.remove(r)
+            # from here on the requests run: a cancel that won the race drops its request
+            group = [r for r in group if r.future.set_running_or_notify_cancel()]
+            if not group:
+                return self._next_job() if self._pending else None
+            if group[0] is not head:
+                head = group[0]
+                footprint = sum(self.backend.request_bytes(r) for r in group) + \
+                    (0 if cached else self.backend.build_bytes(head))
             weights = self.cache.acquire(head.key) if cached else None
             if not cached:
                 self.cache.misses += 1

@@ -131,3 +131,18 @@ def test_hash64x2_equals_two_hash64():
             one = ctypes.c_uint64()
             assert L.rg_hash64(ctypes.c_void_p(a.ctypes.data), n, seed, ctypes.byref(one)) == _lib.RG_OK
             assert got == one.value
+
+
+def test_debug_library_builds_with_every_symbol():
+    """The RG_DEBUG variant (bounds-checked grid reads in the builds) compiles
+    and exports every entry point the header declares."""
+    import ctypes
+
+    from regridding_gb300 import _build
+
+    path = _build.build(debug=True)
+    assert path == _build.LIB_DEBUG
+    dbg = ctypes.CDLL(path)
+    for name in declared_symbols():
+        assert hasattr(dbg, name), name
+    assert dbg.rg_version() == _lib.load().rg_version()

@@ -178,6 +178,87 @@ def test_build_failure_reaches_every_waiting_request():
         assert good.result(5).shape == (1, 9)
 
 
+def test_cancelled_requests_never_run():
+    """Fault injection on the host: a client cancels queued requests.  A
+    request cancelled before admission is dropped (its future reports
+    cancelled, the backend never sees it); the others still run and are
+    batched as usual; an admitted request can no longer be cancelled."""
+    gate = threading.Event()
+    be = FakeBackend(gate=gate)
+    gi, go = grids(4, 3)
+    with RegridServer(hbm_budget=10**9, slots=1, backend=be) as srv:
+        f0 = srv.submit(gi, go, np.ones((1, 4, 4)), key="g")  # holds the only slot
+        time.sleep(0.1)
+        assert not f0.cancel()  # running
+        waiting = [srv.submit(gi, go, np.full((1, 4, 4), k), key="g") for k in range(4)]
+        other = srv.submit(gi, go, np.ones((1, 4, 4)), key="h")
+        time.sleep(0.05)
+        assert waiting[1].cancel() and waiting[3].cancel()
+        gate.set()
+        f0.result(5)
+        kept = [waiting[0].result(5), waiting[2].result(5)]
+        other.result(5)
+        st = srv.stats()
+    assert waiting[1].cancelled() and waiting[3].cancelled()
+    m = FakeBackend.matrix("g", 16, 9)
+    np.testing.assert_array_equal(kept[1], np.full((1, 16), 2.0) @ m.T)
+    assert sum(len(b) for b in be.batches) == 4  # f0, waiting[0], waiting[2], other
+    assert st["cancelled"] == 2 and st["done"] == 4
+
+
+class FlakyAllocBackend(FakeBackend):
+    """A backend whose device allocations fail on chosen calls, as
+    cudaMallocAsync does when the device is out of memory."""
+
+    def __init__(self, fail_build_calls=(), fail_run_calls=(), **kw):
+        super().__init__(**kw)
+        self.fail_build_calls, self.fail_run_calls = set(fail_build_calls), set(fail_run_calls)
+        self.n_build = self.n_run = 0
+
+    def build(self, slot, req):
+        with self.lock:
+            self.n_build += 1
+            fail = self.n_build in self.fail_build_calls
+        if fail:
+            raise MemoryError("cudaMallocAsync: out of memory (injected)")
+        return super().build(slot, req)
+
+    def run(self, slot, m, reqs):
+        with self.lock:
+            self.n_run += 1
+            fail = self.n_run in self.fail_run_calls
+        if fail:
+            raise MemoryError("cudaMallocAsync: out of memory (injected)")
+        return super().run(slot, m, reqs)
+
+
+def test_allocation_failures_fail_their_request_alone():
+    """Fault injection on the host: an allocation fails inside an admitted
+    request's build, and another inside an apply.  Each fails its own
+    request with the error; the reserved device footprint is given back (the
+    server's accounting returns to the cache alone), the failed grid is
+    built again by its next request, and other requests are unaffected."""
+    be = FlakyAllocBackend(fail_build_calls={1}, fail_run_calls={2})
+    gi, go = grids(4, 3)
+    with RegridServer(hbm_budget=10**9, slots=1, backend=be) as srv:
+        first = srv.submit(gi, go, np.ones((1, 4, 4)), key="a")  # build 1 fails
+        with pytest.raises(MemoryError, match="injected"):
+            first.result(5)
+        assert srv._transient == 0 and "a" not in srv.cache
+        ok = srv.submit(gi, go, np.ones((1, 4, 4)), key="a")  # build 2 succeeds, run 1
+        ok.result(5)
+        bad_run = srv.submit(gi, go, np.ones((1, 4, 4)), key="a")  # cached, run 2 fails
+        with pytest.raises(MemoryError, match="injected"):
+            bad_run.result(5)
+        again = srv.submit(gi, go, np.ones((1, 4, 4)), key="a")  # run 3
+        np.testing.assert_array_equal(again.result(5), np.ones((1, 16)) @ FakeBackend.matrix("a", 16, 9).T)
+        with srv._cv:
+            assert srv._transient == 0 and srv.cache.used == srv._in_use()
+        st = srv.stats()
+    assert be.builds == ["a"]  # the failed build never reached the cache; the second one did
+    assert st["builds"] == 1 and st["done"] == 4
+
+
 def test_bad_request_and_close():
     be = FakeBackend(run_delay=0.02)
     gi, go = grids(3, 3)

@@ -29,13 +29,20 @@ namespace {
 
 enum : unsigned { FLAG_NONCONVEX = 1u << 8, FLAG_DEGENERATE = 1u << 9 };
 
+// A vertex of the clipped polygon, 40 bytes (two arrays of 12 per thread):
+// a crossing keeps its parameter t and the reciprocal of its carriers'
+// cross product, from which the gradient pass rebuilds the normal.
 struct PV {
     double x, y;
+    double t, inv;       // crossing data (kind 2): t along output edge e; 1 / cross(r, s)
     signed char ca, cb;  // carrier lines: 0..3 output edges, 4..7 input edges
     signed char kind;    // 0 output vertex (e), 1 input-only, 2 crossing (e, f)
     signed char e;
-    double t, nx, ny, rx, ry;  // crossing data (kind 2)
 };
+
+// float or double values as double (float: exactly, on the integer pipe)
+__device__ __forceinline__ double as_double(float v) { return widen(v); }
+__device__ __forceinline__ double as_double(double v) { return v; }
 
 __device__ __forceinline__ double cross2(double ax, double ay, double bx, double by) { return ax * by - ay * bx; }
 
@@ -89,9 +96,13 @@ __device__ PV crossing(const Quad& O, const Quad& C, int L, int f, bool* ok) {
         rx = C.x[(g + 1) & 3] - ax, ry = C.y[(g + 1) & 3] - ay;
     }
     const double den = cross2(rx, ry, sx, sy);
-    double t = 0;
-    if (den != 0) t = cross2(cx - ax, cy - ay, sx, sy) / den;
-    else *ok = false;
+    double t = 0, inv = 0;
+    if (den != 0) {
+        inv = 1.0 / den;  // one division serves t and (at the gradient) the normal
+        t = cross2(cx - ax, cy - ay, sx, sy) * inv;
+    } else {
+        *ok = false;
+    }
     v.x = ax + t * rx;
     v.y = ay + t * ry;
     v.ca = (signed char)L;
@@ -100,14 +111,11 @@ __device__ PV crossing(const Quad& O, const Quad& C, int L, int f, bool* ok) {
         v.kind = 2;
         v.e = (signed char)L;
         v.t = t;
-        v.nx = den != 0 ? -sy / den : 0;
-        v.ny = den != 0 ? sx / den : 0;
-        v.rx = rx;
-        v.ry = ry;
+        v.inv = inv;
     } else {
         v.kind = 1;
         v.e = -1;
-        v.t = v.nx = v.ny = v.rx = v.ry = 0;
+        v.t = v.inv = 0;
     }
     return v;
 }
@@ -131,7 +139,7 @@ __global__ void __launch_bounds__(128)
     for (int64_t k = row_ptr[o]; k < row_ptr[o + 1]; k++) {
         const int64_t i = col[k];
         double G = 0;
-        for (int64_t d = 0; d < stack; d++) G += (double)gout[d * n_out + o] * (double)values[d * n_in + i];
+        for (int64_t d = 0; d < stack; d++) G = fma(as_double(gout[d * n_out + o]), as_double(values[d * n_in + i]), G);
         if (G == 0 && w_check == nullptr) continue;
         const int64_t ii = i / ncyi, ji = i - ii * ncyi;
         Quad C;
@@ -152,7 +160,7 @@ __global__ void __launch_bounds__(128)
             p.cb = (signed char)v;
             p.kind = 0;
             p.e = (signed char)v;
-            p.t = p.nx = p.ny = p.rx = p.ry = 0;
+            p.t = p.inv = 0;
         }
         int cur = 0;
         bool ok = true;
@@ -201,8 +209,13 @@ __global__ void __launch_bounds__(128)
                 ax[q.e] += Gx;
                 ay[q.e] += Gy;
             } else {
-                const double gr = Gx * q.rx + Gy * q.ry;
-                const double hx = Gx + gr * q.nx, hy = Gy + gr * q.ny;
+                // the crossing of output edge e (r = b - a) with input edge f
+                // (s): n = (-s.y, s.x) / cross(r, s)
+                const int e0 = q.e, e1 = (q.e + 1) & 3, f0 = q.cb - 4, f1 = (q.cb - 3) & 3;
+                const double rx = O.x[e1] - O.x[e0], ry = O.y[e1] - O.y[e0];
+                const double nx = -(C.y[f1] - C.y[f0]) * q.inv, ny = (C.x[f1] - C.x[f0]) * q.inv;
+                const double gr = Gx * rx + Gy * ry;
+                const double hx = Gx + gr * nx, hy = Gy + gr * ny;
                 const int a = q.e, b = (q.e + 1) & 3;
                 ax[a] += (1 - q.t) * hx;
                 ay[a] += (1 - q.t) * hy;

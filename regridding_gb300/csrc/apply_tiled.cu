@@ -573,27 +573,6 @@ __global__ void __launch_bounds__(PATCH * PATCH)
     perm[p * (PATCH * PATCH) + t] = (uint8_t)(key[t] & 255u);
 }
 
-// float32 -> float64, exactly, with integer operations only (the FP64 pipe
-// of a GB300 issues 2 operations per clock per SM and is kept for the sums):
-// a normal binary32 value keeps its sign, its exponent is rebiased from 127
-// to 1023 and its 23 fraction bits are followed by 29 zeros; a subnormal
-// man * 2^-149 is normalised at its leading bit; zeros keep their sign;
-// infinities and NaNs keep their payload under the all-ones exponent.
-__device__ __forceinline__ double widen(float f) {
-    const unsigned u = __float_as_uint(f);
-    const unsigned ex = (u >> 23) & 0xffu, man = u & 0x7fffffu;
-    unsigned long long e64 = 0ull, m64 = 0ull;
-    if (ex != 0u) {
-        e64 = ex == 0xffu ? 0x7ffull : (unsigned long long)(ex + (1023u - 127u));
-        m64 = (unsigned long long)man << 29;
-    } else if (man != 0u) {
-        const int lead = 31 - __clz((int)man);  // 0..22
-        e64 = (unsigned long long)(lead + 1023 - 149);
-        m64 = ((unsigned long long)man << (52 - lead)) & 0xfffffffffffffull;
-    }
-    return __longlong_as_double((long long)(((unsigned long long)(u >> 31) << 63) | (e64 << 52) | m64));
-}
-
 // Whether a float32 is finite, from its exponent bits.
 __device__ __forceinline__ bool finite_bits(float f) {
     return (__float_as_uint(f) & 0x7f800000u) != 0x7f800000u;

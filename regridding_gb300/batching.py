@@ -7,7 +7,7 @@
 * ``ApplyGraph`` replays a fixed set of applies (one per pair, each with its
   own stack) through one captured CUDA graph: after a first eager pass (which
   makes every handle's lazily built state and runs the apply autotuner) the
-  whole set is a single graph launch.
+  whole set is a single graph launch, its applies in parallel chains.
 * ``autotune_sweep_chunk`` times the build of a sample batch for several
   chunk lengths of the parallel walk and keeps the fastest
   (``rg_set_sweep_chunk``); the apply kernels tune themselves per handle.
@@ -35,9 +35,16 @@ class ApplyGraph:
     """A fixed list of applies ``(weights, values, out)`` (device tensors of
     shape ``(stack, n_in)`` and ``(stack, n_out)``) captured once into a CUDA
     graph and replayed with :meth:`replay`.  Inputs are read from, and
-    results written to, the same tensors at every replay."""
+    results written to, the same tensors at every replay.
 
-    def __init__(self, items, accumulate: str = "fast"):
+    The applies are independent, so the graph holds them as ``branches``
+    parallel chains (the capturing stream forks to side streams through
+    events and joins them at the end); each apply goes to the chain with the
+    fewest bytes so far, largest first.  Small applies then run side by side
+    instead of one after another.  Every apply computes what it computes
+    alone, so the results do not depend on ``branches``."""
+
+    def __init__(self, items, accumulate: str = "fast", branches: int = 8):
         torch = _device.torch()
         self.items = list(items)
         self.accumulate = accumulate
@@ -45,13 +52,36 @@ class ApplyGraph:
         for dw, v, o in self.items:
             dw.apply(v, out=o, accumulate=accumulate)
         torch.cuda.synchronize()
+        self.branches = max(1, min(int(branches), len(self.items)))
+        nbytes = [v.numel() * v.element_size() + o.numel() * o.element_size() + dw.nnz * 12
+                  for dw, v, o in self.items]
+        chains = [[] for _ in range(self.branches)]
+        load = [0] * self.branches
+        for k in sorted(range(len(self.items)), key=lambda k: -nbytes[k]):
+            c = load.index(min(load))
+            chains[c].append(k)
+            load[c] += nbytes[k]
+        self.chains = [sorted(c) for c in chains]
         self.graph = torch.cuda.CUDAGraph()
         side = torch.cuda.Stream()
+        forks = [torch.cuda.Stream() for _ in range(self.branches - 1)]
         side.wait_stream(torch.cuda.current_stream())
         with torch.cuda.stream(side):
             with torch.cuda.graph(self.graph, stream=side):
-                for dw, v, o in self.items:
-                    dw.apply(v, out=o, accumulate=accumulate)
+                fork = torch.cuda.Event()
+                fork.record(side)
+                streams = [side] + forks
+                for st in forks:
+                    st.wait_event(fork)
+                for st, chain in zip(streams, self.chains):
+                    with torch.cuda.stream(st):
+                        for k in chain:
+                            dw, v, o = self.items[k]
+                            dw.apply(v, out=o, accumulate=accumulate)
+                for st in forks:
+                    join = torch.cuda.Event()
+                    join.record(st)
+                    side.wait_event(join)
         torch.cuda.current_stream().wait_stream(side)
 
     def replay(self) -> None:

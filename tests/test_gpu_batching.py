@@ -81,7 +81,10 @@ def test_chunk_length_does_not_change_weights(torch, chunk):
         assert same_weights(r, w.export_numpy())
 
 
-def test_apply_graph_replays_the_eager_applies(torch):
+@pytest.mark.parametrize("branches", [1, 3, 8])
+def test_apply_graph_replays_the_eager_applies(torch, branches):
+    """The graph (its applies in 1, 3 or 8 parallel chains) gives the eager
+    applies' results bit for bit, and reads new inputs at every replay."""
     from regridding_gb300 import batching
 
     pairs = uneven_pairs(10, seed=24)
@@ -93,7 +96,8 @@ def test_apply_graph_replays_the_eager_applies(torch):
         v = torch.from_numpy(rng.poisson(50, (stack, dw.n_in)).astype(np.float32)).cuda()
         o = torch.empty((stack, dw.n_out), dtype=torch.float32, device="cuda")
         items.append((dw, v, o))
-    graph = batching.ApplyGraph(items)
+    graph = batching.ApplyGraph(items, branches=branches)
+    assert sorted(k for c in graph.chains for k in c) == list(range(len(items)))
     eager = [dw.apply(v, accumulate="fast").cpu().numpy() for dw, v, _ in items]
     for _, _, o in items:
         o.zero_()

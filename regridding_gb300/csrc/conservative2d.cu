@@ -298,85 +298,31 @@ __device__ void locate_brute_warp(const Grid& g, double px, double py, int64_t* 
 
 // grid_volume: _grids.py:50-140.  One thread per cell; the four contour terms
 // are added in the upstream order (((0 - A) + B) - C) + D.
+__device__ __forceinline__ double cell_area_at(const double* __restrict__ x, const double* __restrict__ y,
+                                               int64_t ny, int64_t p, int64_t q) {
+    double x00 = x[p * ny + q], y00 = y[p * ny + q];
+    double x10 = x[(p + 1) * ny + q], y10 = y[(p + 1) * ny + q];
+    double x01 = x[p * ny + q + 1], y01 = y[p * ny + q + 1];
+    double x11 = x[(p + 1) * ny + q + 1], y11 = y[(p + 1) * ny + q + 1];
+    // axis 0 (transposed, coordinates swapped)
+    double A = dmul(dsub(dmul(y00, x10), dmul(y10, x00)), 0.5);
+    double B = dmul(dsub(dmul(y01, x11), dmul(y11, x01)), 0.5);
+    // axis 1
+    double C = dmul(dsub(dmul(x00, y01), dmul(x01, y00)), 0.5);
+    double D = dmul(dsub(dmul(x10, y11), dmul(x11, y10)), 0.5);
+    double v = dsub(0.0, A);
+    v = dadd(v, B);
+    v = dsub(v, C);
+    v = dadd(v, D);
+    return v;
+}
+
 __global__ void cell_area_kernel(const double* __restrict__ x, const double* __restrict__ y,
                                  int64_t nx, int64_t ny, double* __restrict__ out) {
     int64_t ncx = nx - 1, ncy = ny - 1;
     for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncx * ncy;
-         c += (int64_t)gridDim.x * blockDim.x) {
-        int64_t p = c / ncy, q = c % ncy;
-        double x00 = x[p * ny + q], y00 = y[p * ny + q];
-        double x10 = x[(p + 1) * ny + q], y10 = y[(p + 1) * ny + q];
-        double x01 = x[p * ny + q + 1], y01 = y[p * ny + q + 1];
-        double x11 = x[(p + 1) * ny + q + 1], y11 = y[(p + 1) * ny + q + 1];
-        // axis 0 (transposed, coordinates swapped)
-        double A = dmul(dsub(dmul(y00, x10), dmul(y10, x00)), 0.5);
-        double B = dmul(dsub(dmul(y01, x11), dmul(y11, x01)), 0.5);
-        // axis 1
-        double C = dmul(dsub(dmul(x00, y01), dmul(x01, y00)), 0.5);
-        double D = dmul(dsub(dmul(x10, y11), dmul(x11, y10)), 0.5);
-        double v = dsub(0.0, A);
-        v = dadd(v, B);
-        v = dsub(v, C);
-        v = dadd(v, D);
-        out[c] = v;
-    }
-}
-
-// Bounding box (xmin, ymin, xmax, ymax) of a vertex grid: per-block partial
-// extrema, then one block combines them (min/max are exact in any order).
-__global__ void bbox_partial(const double* __restrict__ x, const double* __restrict__ y, int64_t n,
-                             double* __restrict__ part) {
-    __shared__ double s[4][256];
-    double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        double xv = x[k], yv = y[k];
-        a = fmin(a, xv);
-        b = fmin(b, yv);
-        c = fmax(c, xv);
-        d = fmax(d, yv);
-    }
-    s[0][threadIdx.x] = a;
-    s[1][threadIdx.x] = b;
-    s[2][threadIdx.x] = c;
-    s[3][threadIdx.x] = d;
-    __syncthreads();
-    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
-        if ((int)threadIdx.x < w) {
-            s[0][threadIdx.x] = fmin(s[0][threadIdx.x], s[0][threadIdx.x + w]);
-            s[1][threadIdx.x] = fmin(s[1][threadIdx.x], s[1][threadIdx.x + w]);
-            s[2][threadIdx.x] = fmax(s[2][threadIdx.x], s[2][threadIdx.x + w]);
-            s[3][threadIdx.x] = fmax(s[3][threadIdx.x], s[3][threadIdx.x + w]);
-        }
-        __syncthreads();
-    }
-    if (threadIdx.x < 4) part[blockIdx.x * 4 + threadIdx.x] = s[threadIdx.x][0];
-}
-
-// one warp: each lane folds a stride of the partials, then a shuffle tree
-__global__ void bbox_combine(const double* __restrict__ part, int nparts, double* __restrict__ out4) {
-    const int lane = threadIdx.x & 31;
-    if (threadIdx.x >= 32) return;
-    double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
-    for (int k = lane; k < nparts; k += 32) {
-        a = fmin(a, part[4 * k]);
-        b = fmin(b, part[4 * k + 1]);
-        c = fmax(c, part[4 * k + 2]);
-        d = fmax(d, part[4 * k + 3]);
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
-        b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
-        c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
-        d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
-    }
-    if (lane == 0) {
-        out4[0] = a;
-        out4[1] = b;
-        out4[2] = c;
-        out4[3] = d;
-    }
+         c += (int64_t)gridDim.x * blockDim.x)
+        out[c] = cell_area_at(x, y, ny, c / ncy, c % ncy);
 }
 
 // Boundary edges in the scan order of _step_outside_static (:608-683):
@@ -389,46 +335,43 @@ struct Edge {
     int pad;
 };
 
-__global__ void boundary_edges_kernel(Grid g, Edge* edges, int64_t nedges) {
-    int64_t ncx = g.nx - 1, ncy = g.ny - 1;
-    for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nedges;
-         k += (int64_t)gridDim.x * blockDim.x) {
-        int axis, dir;
-        int64_t i0, kk = k;
-        if (kk < 2 * ncy) {
-            axis = 0;
-            dir = kk >= ncy;
-            i0 = kk - dir * ncy;
-        } else {
-            kk -= 2 * ncy;
-            axis = 1;
-            dir = kk >= ncx;
-            i0 = kk - dir * ncx;
-        }
-        Edge e;
-        if (axis == 0) {
-            int64_t ie = dir ? g.nx - 1 : 0;
-            e.x3 = g.X(ie, i0); e.y3 = g.Y(ie, i0);
-            e.x4 = g.X(ie, i0 + 1); e.y4 = g.Y(ie, i0 + 1);
-            int64_t cx = dir ? ncx - 1 : 0;
-            e.cell = cx * ncy + i0;
-        } else {
-            int64_t je = dir ? g.ny - 1 : 0;
-            e.x3 = g.X(i0, je); e.y3 = g.Y(i0, je);
-            e.x4 = g.X(i0 + 1, je); e.y4 = g.Y(i0 + 1, je);
-            int64_t cy = dir ? ncy - 1 : 0;
-            e.cell = i0 * ncy + cy;
-        }
-        e.code = dir * 2 + axis;
-        e.pad = 0;
-        edges[k] = e;
+__device__ __forceinline__ Edge boundary_edge(const Grid& g, int64_t k) {
+    const int64_t ncx = g.nx - 1, ncy = g.ny - 1;
+    int axis, dir;
+    int64_t i0, kk = k;
+    if (kk < 2 * ncy) {
+        axis = 0;
+        dir = kk >= ncy;
+        i0 = kk - dir * ncy;
+    } else {
+        kk -= 2 * ncy;
+        axis = 1;
+        dir = kk >= ncx;
+        i0 = kk - dir * ncx;
     }
+    Edge e;
+    if (axis == 0) {
+        int64_t ie = dir ? g.nx - 1 : 0;
+        e.x3 = g.X(ie, i0); e.y3 = g.Y(ie, i0);
+        e.x4 = g.X(ie, i0 + 1); e.y4 = g.Y(ie, i0 + 1);
+        int64_t cx = dir ? ncx - 1 : 0;
+        e.cell = cx * ncy + i0;
+    } else {
+        int64_t je = dir ? g.ny - 1 : 0;
+        e.x3 = g.X(i0, je); e.y3 = g.Y(i0, je);
+        e.x4 = g.X(i0 + 1, je); e.y4 = g.Y(i0 + 1, je);
+        int64_t cy = dir ? ncy - 1 : 0;
+        e.cell = i0 * ncy + cy;
+    }
+    e.code = dir * 2 + axis;
+    e.pad = 0;
+    return e;
 }
 
 struct Bins {
     double ox, oy, inv_h;
     int nbx, nby;
-    const int32_t* ptr;    // [nbx*nby + 1]
+    const int32_t* ptr;    // [nbx*nby + 1] offsets into items
     const int32_t* items;  // edge indices
 };
 
@@ -439,21 +382,142 @@ __device__ __forceinline__ int bin_coord(double v, double o, double inv_h, int n
     return (int)f;
 }
 
+// Static-grid preparation of a whole batch.  The static grids are the input
+// and the output grid of every pair (grid 2g and 2g + 1 for pair g); they
+// share batch-wide arrays, so that every stage below is one launch whatever
+// the number of pairs.  Grid k's boundary edges start at edge_base; its
+// nbins + 1 bin slots (the last one always empty, so that the grid's slots
+// end on its own total) start at bin_base.  Its bins hold offsets into the
+// batch's one item array, and its items are edge indices of the grid.
+struct PrepGrid {
+    Grid g;
+    Bins b;
+    int64_t cell_base;  // first cell of the pair's input grid in area_in (even k only)
+    int64_t edge_base;
+    int64_t bin_base;
+};
+
+// grid k whose edges hold batch edge e (edge bases rise strictly: a grid has
+// at least four boundary edges)
+__device__ __forceinline__ int grid_of_edge(const PrepGrid* __restrict__ P, int n, int64_t e) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (P[mid].edge_base <= e) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// areas of the input cells of every pair, in area_in's order (pair by pair)
+__global__ void cell_area_batch(const PrepGrid* __restrict__ P, int G, int64_t ncells, double* __restrict__ out) {
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < ncells;
+         c += (int64_t)gridDim.x * blockDim.x) {
+        int lo = 0, hi = G - 1;
+        while (lo < hi) {
+            const int mid = (lo + hi + 1) >> 1;
+            if (P[2 * mid].cell_base <= c) lo = mid;
+            else hi = mid - 1;
+        }
+        const Grid g = P[2 * lo].g;
+        const int64_t local = c - P[2 * lo].cell_base, ncy = g.ny - 1;
+        out[c] = cell_area_at(g.x, g.y, g.ny, local / ncy, local % ncy);
+    }
+}
+
+// Bounding boxes (xmin, ymin, xmax, ymax) of every static grid: nparts
+// blocks of 256 threads per grid fold strided vertices into partial
+// extrema, then one warp per grid combines them (min and max are exact in
+// any order, so the partition does not matter).
+__global__ void __launch_bounds__(256) bbox_partial_batch(const PrepGrid* __restrict__ P, int nparts,
+                                                          double* __restrict__ part) {
+    __shared__ double sh[4][256];
+    const int k = blockIdx.x / nparts, p = blockIdx.x % nparts;
+    const Grid g = P[k].g;
+    const int64_t n = g.nx * g.ny;
+    double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+    for (int64_t v = (int64_t)p * blockDim.x + threadIdx.x; v < n; v += (int64_t)nparts * blockDim.x) {
+        const double xv = g.x[v], yv = g.y[v];
+        a = fmin(a, xv);
+        b = fmin(b, yv);
+        c = fmax(c, xv);
+        d = fmax(d, yv);
+    }
+    sh[0][threadIdx.x] = a;
+    sh[1][threadIdx.x] = b;
+    sh[2][threadIdx.x] = c;
+    sh[3][threadIdx.x] = d;
+    __syncthreads();
+    for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+        if ((int)threadIdx.x < w) {
+            sh[0][threadIdx.x] = fmin(sh[0][threadIdx.x], sh[0][threadIdx.x + w]);
+            sh[1][threadIdx.x] = fmin(sh[1][threadIdx.x], sh[1][threadIdx.x + w]);
+            sh[2][threadIdx.x] = fmax(sh[2][threadIdx.x], sh[2][threadIdx.x + w]);
+            sh[3][threadIdx.x] = fmax(sh[3][threadIdx.x], sh[3][threadIdx.x + w]);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x < 4) part[((int64_t)k * nparts + p) * 4 + threadIdx.x] = sh[threadIdx.x][0];
+}
+
+__global__ void bbox_combine_batch(const double* __restrict__ part, int nparts, int ngrids, double* __restrict__ out) {
+    const int k = (int)((blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5), lane = threadIdx.x & 31;
+    if (k >= ngrids) return;  // whole warps leave together
+    const double* q = part + (int64_t)k * nparts * 4;
+    double a = INFINITY, b = INFINITY, c = -INFINITY, d = -INFINITY;
+    for (int i = lane; i < nparts; i += 32) {
+        a = fmin(a, q[4 * i]);
+        b = fmin(b, q[4 * i + 1]);
+        c = fmax(c, q[4 * i + 2]);
+        d = fmax(d, q[4 * i + 3]);
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        a = fmin(a, __shfl_xor_sync(0xffffffffu, a, o));
+        b = fmin(b, __shfl_xor_sync(0xffffffffu, b, o));
+        c = fmax(c, __shfl_xor_sync(0xffffffffu, c, o));
+        d = fmax(d, __shfl_xor_sync(0xffffffffu, d, o));
+    }
+    if (lane == 0) {
+        out[4 * k] = a;
+        out[4 * k + 1] = b;
+        out[4 * k + 2] = c;
+        out[4 * k + 3] = d;
+    }
+}
+
+__global__ void boundary_edges_batch(const PrepGrid* __restrict__ P, int ngrids, int64_t nedges,
+                                     Edge* __restrict__ edges) {
+    for (int64_t e = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; e < nedges;
+         e += (int64_t)gridDim.x * blockDim.x) {
+        const int k = grid_of_edge(P, ngrids, e);
+        edges[e] = boundary_edge(P[k].g, e - P[k].edge_base);
+    }
+}
+
+// Every edge goes to each bin its bounding box touches: a counting pass,
+// then (after the scan of the counts) a filing pass.  The order of the
+// items within a bin depends on the atomics; the outside step that reads
+// them is order-independent.
 template <bool FILL>
-__global__ void bin_edges_kernel(const Edge* edges, int64_t nedges, Bins b, unsigned* counts,
-                                 int32_t* items, const int64_t* ptr64) {
+__global__ void bin_edges_batch(const PrepGrid* __restrict__ P, int ngrids, const Edge* __restrict__ edges,
+                                int64_t nedges, unsigned* __restrict__ counts, int32_t* __restrict__ items,
+                                const int64_t* __restrict__ ptr64) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < nedges;
          k += (int64_t)gridDim.x * blockDim.x) {
-        Edge e = edges[k];
+        const int gk = grid_of_edge(P, ngrids, k);
+        const Bins b = P[gk].b;
+        const int64_t base = P[gk].bin_base;
+        const Edge e = edges[k];
         int bx0 = bin_coord(fmin(e.x3, e.x4), b.ox, b.inv_h, b.nbx);
         int bx1 = bin_coord(fmax(e.x3, e.x4), b.ox, b.inv_h, b.nbx);
         int by0 = bin_coord(fmin(e.y3, e.y4), b.oy, b.inv_h, b.nby);
         int by1 = bin_coord(fmax(e.y3, e.y4), b.oy, b.inv_h, b.nby);
         for (int by = by0; by <= by1; by++)
             for (int bx = bx0; bx <= bx1; bx++) {
-                int64_t bin = (int64_t)by * b.nbx + bx;
+                const int64_t bin = base + (int64_t)by * b.nbx + bx;
                 unsigned pos = atomicAdd(&counts[bin], 1u);
-                if (FILL) items[ptr64[bin] + pos] = (int32_t)k;
+                if (FILL) items[ptr64[bin] + pos] = (int32_t)(k - P[gk].edge_base);
             }
     }
 }
@@ -1153,44 +1217,18 @@ __global__ void compact_rows(const int64_t* __restrict__ bptr, const int64_t* __
     }
 }
 
-// Static-grid preparation in two halves so that a batch synchronises once
-// for all its grids: the first half fills the boundary edges, sizes the
-// bins and counts the edges of every bin (the total lands in *total_dev);
-// the second, after the caller has read the totals, files the edges.
-struct StaticPrep {
-    Edge* edges = nullptr;
-    unsigned* counts = nullptr;
-    int64_t* ptr64 = nullptr;
-    int32_t* ptr32 = nullptr;
-    int32_t* items = nullptr;
-    int64_t nedges = 0, nbins = 0;
-};
-
-int prepare_static_count(const double* x, const double* y, int64_t nx, int64_t ny, const double* bbox_h, Static* S,
-                         StaticPrep* R, int64_t* total_dev, cudaStream_t s) {
-    S->g = Grid{x, y, nx, ny};
-    S->ncx = nx - 1;
-    S->ncy = ny - 1;
-    S->blx = bbox_h[0];
-    S->bly = bbox_h[1];
-    S->bux = bbox_h[2];
-    S->buy = bbox_h[3];
-    S->nbound = 2 * (nx - 1) + 2 * (ny - 1);
-    const int64_t nedges = 2 * S->ncy + 2 * S->ncx;
-    R->nedges = nedges;
-    RG_TRY(dalloc(&R->edges, (size_t)nedges, s));
-    boundary_edges_kernel<<<grid_for(nedges, 128), 128, 0, s>>>(S->g, R->edges, nedges);
-    S->edges = R->edges;
-    // bins: square, sized so that a bin holds about one edge along the boundary
-    double ex = S->bux - S->blx, ey = S->buy - S->bly;
-    double ext = ex > ey ? ex : ey;
+// Bins of a static grid with bounding box bb: square, sized so that a bin
+// holds about one edge along the boundary; at most 1024 a side.
+Bins static_bins(const double* bb, int64_t nedges) {
+    const double ex = bb[2] - bb[0], ey = bb[3] - bb[1];
+    const double ext = ex > ey ? ex : ey;
     int64_t side = nedges / 8;
     if (side < 8) side = 8;
     if (side > 1024) side = 1024;
-    double hbin = ext > 0 && std::isfinite(ext) ? ext / (double)side : 1.0;
+    const double hbin = ext > 0 && std::isfinite(ext) ? ext / (double)side : 1.0;
     Bins b;
-    b.ox = S->blx;
-    b.oy = S->bly;
+    b.ox = bb[0];
+    b.oy = bb[1];
     b.inv_h = 1.0 / hbin;
     b.nbx = (int)std::min<double>(1024.0, std::max(1.0, std::ceil(ex / hbin)));
     b.nby = (int)std::min<double>(1024.0, std::max(1.0, std::ceil(ey / hbin)));
@@ -1200,41 +1238,29 @@ int prepare_static_count(const double* x, const double* y, int64_t nx, int64_t n
     }
     b.ptr = nullptr;
     b.items = nullptr;
-    S->bins = b;
-    const int64_t nbins = (int64_t)b.nbx * b.nby;
-    R->nbins = nbins;
-    RG_TRY(dalloc(&R->counts, (size_t)nbins + 1, s));
-    RG_TRY(dalloc(&R->ptr64, (size_t)nbins + 1, s));
-    RG_TRY(dalloc(&R->ptr32, (size_t)nbins + 1, s));
-    RG_TRY(zero_async(R->counts, sizeof(unsigned) * (nbins + 1), s));
-    bin_edges_kernel<false><<<grid_for(nedges, 128), 128, 0, s>>>(R->edges, nedges, b, R->counts, nullptr, nullptr);
-    return exclusive_scan_u32_to_i64(R->counts, R->ptr64, nbins + 1, total_dev, s);
+    return b;
 }
 
-int prepare_static_fill(Static* S, StaticPrep* R, int64_t total, cudaStream_t s) {
-    RG_TRY(dalloc(&R->items, (size_t)total, s));
-    RG_TRY(zero_async(R->counts, sizeof(unsigned) * (R->nbins + 1), s));
-    bin_edges_kernel<true><<<grid_for(R->nedges, 128), 128, 0, s>>>(R->edges, R->nedges, S->bins, R->counts,
-                                                                     R->items, R->ptr64);
-    i64_to_i32<<<grid_for(R->nbins + 1, 256), 256, 0, s>>>(R->ptr64, R->ptr32, R->nbins + 1);
-    RG_CUDA(cudaGetLastError());
-    dfree(R->counts, s);
-    dfree(R->ptr64, s);
-    R->counts = nullptr;
-    R->ptr64 = nullptr;
-    S->bins.ptr = R->ptr32;
-    S->bins.items = R->items;
-    return RG_OK;
-}
-
-void free_static(StaticPrep* R, cudaStream_t s) {
-    dfree(R->edges, s);
-    dfree(R->counts, s);
-    dfree(R->ptr64, s);
-    dfree(R->ptr32, s);
-    dfree(R->items, s);
-    *R = StaticPrep();
-}
+// Batch-wide arrays of the static grids' preparation (PrepGrid)
+struct StaticBatch {
+    PrepGrid* grids = nullptr;  // [2G]
+    Edge* edges = nullptr;
+    unsigned* counts = nullptr;
+    int64_t* ptr64 = nullptr;
+    int32_t* ptr32 = nullptr;
+    int32_t* items = nullptr;
+    double* bbox_part = nullptr;
+    void free(cudaStream_t s) {
+        dfree(grids, s);
+        dfree(edges, s);
+        dfree(counts, s);
+        dfree(ptr64, s);
+        dfree(ptr32, s);
+        dfree(items, s);
+        dfree(bbox_part, s);
+        *this = StaticBatch();
+    }
+};
 
 }  // namespace
 
@@ -1536,8 +1562,7 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
     int st = RG_OK;
     double* area_in = nullptr;
     double* bbox_d = nullptr;
-    double* bbox_part = nullptr;
-    std::vector<StaticPrep> prep((size_t)2 * G);
+    StaticBatch SB;
     int64_t* totals = nullptr;
     SweepParams* P_dev = nullptr;
     int64_t *line_base_dev = nullptr, *out_base_dev = nullptr, *chunk_base_dev = nullptr;
@@ -1561,21 +1586,35 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
     void** dst_dev = nullptr;  // [3G]: row_ptr, col, val pointers of every grid
 
     do {
-        // areas of the input cells and bounding boxes of all grids (sync 1)
-        if ((st = dalloc(&area_in, (size_t)in_base[G], s))) break;
-        if ((st = dalloc(&bbox_d, (size_t)8 * G, s))) break;
-        if ((st = dalloc(&bbox_part, 8 * 256, s))) break;
-        for (int g = 0; g < G && st == RG_OK; g++) {
-            const PairSpec& q = pairs[g];
-            st = cell_area_2d(q.xi, q.yi, q.nxi, q.nyi, area_in + in_base[g], s);
-            bbox_partial<<<256, 256, 0, s>>>(q.xi, q.yi, q.nxi * q.nyi, bbox_part);
-            bbox_combine<<<1, 32, 0, s>>>(bbox_part, 256, bbox_d + 8 * g);
-            bbox_partial<<<256, 256, 0, s>>>(q.xo, q.yo, q.nxo * q.nyo, bbox_part + 4 * 256);
-            bbox_combine<<<1, 32, 0, s>>>(bbox_part + 4 * 256, 256, bbox_d + 8 * g + 4);
+        // static grids: the input and the output grid of every pair.  Areas
+        // of the input cells, bounding boxes and boundary edges of all grids
+        // (sync 1 reads the boxes)
+        const int NG = 2 * G;
+        std::vector<PrepGrid> PG((size_t)NG);
+        int64_t nedges_all = 0, max_verts = 0;
+        for (int k = 0; k < NG; k++) {
+            const PairSpec& q = pairs[k >> 1];
+            PrepGrid& r = PG[k];
+            memset(&r, 0, sizeof(PrepGrid));
+            r.g = (k & 1) ? Grid{q.xo, q.yo, q.nxo, q.nyo} : Grid{q.xi, q.yi, q.nxi, q.nyi};
+            r.cell_base = (k & 1) ? 0 : in_base[k >> 1];
+            r.edge_base = nedges_all;
+            nedges_all += 2 * (r.g.nx - 1) + 2 * (r.g.ny - 1);
+            max_verts = std::max(max_verts, r.g.nx * r.g.ny);
         }
-        if (st) break;
-        std::vector<double> bbox_h((size_t)8 * G);
-        small_to_host(bbox_h.data(), bbox_d, sizeof(double) * 8 * G, s);
+        // blocks per grid for the boxes: about 16 vertices a thread, 1..256
+        const int nparts = (int)std::min<int64_t>(256, std::max<int64_t>(1, (max_verts + 4095) / 4096));
+        if ((st = upload(&SB.grids, PG, s))) break;
+        if ((st = dalloc(&area_in, (size_t)in_base[G], s))) break;
+        if ((st = dalloc(&bbox_d, (size_t)4 * NG, s))) break;
+        if ((st = dalloc(&SB.bbox_part, (size_t)4 * NG * nparts, s))) break;
+        if ((st = dalloc(&SB.edges, (size_t)nedges_all, s))) break;
+        cell_area_batch<<<grid_for(in_base[G], 256), 256, 0, s>>>(SB.grids, G, in_base[G], area_in);
+        bbox_partial_batch<<<(unsigned)(NG * nparts), 256, 0, s>>>(SB.grids, nparts, SB.bbox_part);
+        bbox_combine_batch<<<grid_for((int64_t)NG * 32, 128), 128, 0, s>>>(SB.bbox_part, nparts, NG, bbox_d);
+        boundary_edges_batch<<<grid_for(nedges_all, 128), 128, 0, s>>>(SB.grids, NG, nedges_all, SB.edges);
+        std::vector<double> bbox_h((size_t)4 * NG);
+        small_to_host(bbox_h.data(), bbox_d, sizeof(double) * 4 * NG, s);
         cudaError_t e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative build: %s", cudaGetErrorString(e));
@@ -1583,32 +1622,69 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
             break;
         }
 
-        // static grids: boundary edges and bins (sync 2)
-        std::vector<SweepParams> P((size_t)G);
-        if ((st = dalloc(&totals, (size_t)2 * G, s))) break;
-        for (int g = 0; g < G && st == RG_OK; g++) {
-            const PairSpec& q = pairs[g];
-            memset(&P[g], 0, sizeof(SweepParams));
-            st = prepare_static_count(q.xi, q.yi, q.nxi, q.nyi, bbox_h.data() + 8 * g, &P[g].st[0], &prep[2 * g],
-                                      totals + 2 * g, s);
-            if (st == RG_OK)
-                st = prepare_static_count(q.xo, q.yo, q.nxo, q.nyo, bbox_h.data() + 8 * g + 4, &P[g].st[1],
-                                          &prep[2 * g + 1], totals + 2 * g + 1, s);
+        // bins of every static grid: count the edges of each bin, one scan
+        // over the slots of all grids (sync 2 reads the item total), file
+        int64_t nslots = 0;
+        for (int k = 0; k < NG; k++) {
+            PrepGrid& r = PG[k];
+            r.b = static_bins(bbox_h.data() + 4 * k, 2 * (r.g.nx - 1) + 2 * (r.g.ny - 1));
+            r.bin_base = nslots;
+            nslots += (int64_t)r.b.nbx * r.b.nby + 1;
         }
-        if (st) break;
-        std::vector<int64_t> totals_h((size_t)2 * G);
-        small_to_host(totals_h.data(), totals, sizeof(int64_t) * 2 * G, s);
+        if ((st = small_to_device(SB.grids, PG.data(), sizeof(PrepGrid) * PG.size(), s))) break;
+        if ((st = dalloc(&totals, 1, s))) break;
+        if ((st = dalloc(&SB.counts, (size_t)nslots, s))) break;
+        if ((st = dalloc(&SB.ptr64, (size_t)nslots, s))) break;
+        if ((st = dalloc(&SB.ptr32, (size_t)nslots, s))) break;
+        if ((st = zero_async(SB.counts, sizeof(unsigned) * nslots, s))) break;
+        bin_edges_batch<false><<<grid_for(nedges_all, 128), 128, 0, s>>>(SB.grids, NG, SB.edges, nedges_all,
+                                                                          SB.counts, nullptr, nullptr);
+        if ((st = exclusive_scan_u32_to_i64(SB.counts, SB.ptr64, nslots, totals, s))) break;
+        int64_t nitems = 0;
+        small_to_host(&nitems, totals, sizeof(int64_t), s);
         e = cudaStreamSynchronize(s);
         if (e != cudaSuccess) {
             set_error("conservative build: %s", cudaGetErrorString(e));
             st = RG_ERR_CUDA;
             break;
         }
-        for (int g = 0; g < G && st == RG_OK; g++) {
-            st = prepare_static_fill(&P[g].st[0], &prep[2 * g], totals_h[2 * g], s);
-            if (st == RG_OK) st = prepare_static_fill(&P[g].st[1], &prep[2 * g + 1], totals_h[2 * g + 1], s);
+        if (nitems >= (int64_t)INT32_MAX) {
+            set_error("conservative build: %lld binned boundary edges exceed 2^31", (long long)nitems);
+            st = RG_ERR_UNSUPPORTED;
+            break;
         }
-        if (st) break;
+        if ((st = dalloc(&SB.items, (size_t)nitems, s))) break;
+        if ((st = zero_async(SB.counts, sizeof(unsigned) * nslots, s))) break;
+        bin_edges_batch<true><<<grid_for(nedges_all, 128), 128, 0, s>>>(SB.grids, NG, SB.edges, nedges_all,
+                                                                         SB.counts, SB.items, SB.ptr64);
+        i64_to_i32<<<grid_for(nslots, 256), 256, 0, s>>>(SB.ptr64, SB.ptr32, nslots);
+        e = cudaGetLastError();
+        if (e != cudaSuccess) {
+            set_error("conservative build (static grids): %s", cudaGetErrorString(e));
+            st = RG_ERR_CUDA;
+            break;
+        }
+        std::vector<SweepParams> P((size_t)G);
+        for (int g = 0; g < G; g++) {
+            memset(&P[g], 0, sizeof(SweepParams));
+            for (int side = 0; side < 2; side++) {
+                const PrepGrid& r = PG[2 * g + side];
+                const double* bb = bbox_h.data() + 4 * (2 * g + side);
+                Static& S = P[g].st[side];
+                S.g = r.g;
+                S.ncx = r.g.nx - 1;
+                S.ncy = r.g.ny - 1;
+                S.blx = bb[0];
+                S.bly = bb[1];
+                S.bux = bb[2];
+                S.buy = bb[3];
+                S.nbound = 2 * S.ncx + 2 * S.ncy;
+                S.edges = SB.edges + r.edge_base;
+                S.bins = r.b;
+                S.bins.ptr = SB.ptr32 + r.bin_base;
+                S.bins.items = SB.items;
+            }
+        }
 
         // sweep families in upstream order: sweep output (axis 0, 1), sweep
         // input (axis 0, 1); line bases global across the batch
@@ -1809,8 +1885,7 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
 
     dfree(area_in, s);
     dfree(bbox_d, s);
-    dfree(bbox_part, s);
-    for (auto& r : prep) free_static(&r, s);
+    SB.free(s);
     dfree(totals, s);
     dfree(P_dev, s);
     dfree(line_base_dev, s);

@@ -310,6 +310,7 @@ constexpr int PATCH = 16;      // output cells per patch side
 constexpr int PATCH_WARPS = 8; // 4 x 2 warp tiles of 4 x 8
 constexpr int PBOX_C = 32;     // box columns: one 128-byte swizzle span
 constexpr int PBOX_MAX_R = 32; // box rows at most
+constexpr int PLANE = PBOX_MAX_R * PBOX_C;  // floats of one slice's plane in a stage (4 KB)
 
 __device__ __forceinline__ unsigned smem_u32(const void* p) { return (unsigned)__cvta_generic_to_shared(p); }
 
@@ -605,16 +606,61 @@ __device__ __forceinline__ double widen_normal(unsigned u) {
 //              in double once per output.  Entries in the gather order.
 constexpr int MODE_FAST = 0, MODE_EXACT = 1, MODE_FF = 2;
 
-// One float-float step: (h, l) += x * (wh + wl).
-__device__ __forceinline__ void ff_step(float& h, float& l, float wh, float wl, float x) {
-    const float p = __fmul_rn(x, wh);
-    const float e = __fmaf_rn(x, wh, -p);      // x * wh - p, exactly
-    const float r = __fmaf_rn(x, wl, e);       // the product's low part
-    const float t = __fadd_rn(h, p);           // two-sum of h and p: t + err = h + p exactly
-    const float bp = __fsub_rn(t, h);
-    const float err = __fadd_rn(__fsub_rn(h, __fsub_rn(t, bp)), __fsub_rn(p, bp));
+// Packed pairs of float32 (two slices of one output): the sm_100-family
+// f32x2 instructions apply one IEEE operation, rounded to nearest, to both
+// halves, at the issue cost of one scalar instruction.
+__device__ __forceinline__ uint64_t f2_pack(float a, float b) {
+    uint64_t r;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float2 f2_unpack(uint64_t v) {
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(v));
+    return r;
+}
+__device__ __forceinline__ uint64_t f2_add(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_sub(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_mul(uint64_t a, uint64_t b) {
+    uint64_t d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ uint64_t f2_fma(uint64_t a, uint64_t b, uint64_t c) {
+    uint64_t d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+    return d;
+}
+
+// One float-float step on a pair of slices: (h, l) += x * (wh + wl), with
+// the weight given as the pairs wh, -wh and wl.  Per half the operations
+// and their results are those of the scalar step
+//     p = x wh;  e = fma(x, wh, -p);  r = fma(x, wl, e);
+//     t = h + p;  bp = t - h;  err = (h - (t - bp)) + (p - bp);
+//     h = t;  l = l + (err + r)
+// (Dekker's product, Knuth's two-sum), written with pn = x (-wh) = -p so
+// that no operand needs negating: fma(x, wh, pn) = x wh - p, h - pn = h + p,
+// and p - bp = -(pn + bp), subtracted from h - (t - bp).  (The only
+// difference is the sign of an exact zero p - bp, which cannot reach the
+// sum: h - (t - bp) is never -0, as h starts at +0.)
+__device__ __forceinline__ void ff_step2(uint64_t& h, uint64_t& l, uint64_t wh, uint64_t whn, uint64_t wl,
+                                         uint64_t x) {
+    const uint64_t pn = f2_mul(x, whn);
+    const uint64_t e = f2_fma(x, wh, pn);
+    const uint64_t r = f2_fma(x, wl, e);
+    const uint64_t t = f2_sub(h, pn);
+    const uint64_t bp = f2_sub(t, h);
+    const uint64_t err = f2_sub(f2_sub(h, f2_sub(t, bp)), f2_add(pn, bp));
     h = t;
-    l = __fadd_rn(l, __fadd_rn(err, r));
+    l = f2_add(l, f2_add(err, r));
 }
 
 template <int SPS, int NST, int MINB, int MODE, int CT = CACHED_T>
@@ -624,12 +670,20 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                     const float* __restrict__ bval, const float* __restrict__ blo, const float* __restrict__ val,
                     const double* __restrict__ dval, double* __restrict__ vout64, FastDiv nd,
                     PatchGrid P, int64_t n_patches, const int2* __restrict__ origin, int BR, int stage_floats,
-                    unsigned stage_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
+                    unsigned box_bytes, const float* __restrict__ vin, int64_t n_in, float* __restrict__ vout,
                     int64_t n_out, int64_t stack, int64_t chunk, unsigned* __restrict__ flags,
                     const uint8_t* __restrict__ perm) {
     constexpr bool EXACT = MODE == MODE_EXACT;
     constexpr bool OUT64 = MODE != MODE_FAST;
+    // The float64-output modes give every slice of a stage its own 4 KB plane
+    // (constant gather offsets; one box copy per slice) and let the last warp
+    // done with a stage refill it.  The float32 mode, whose gathers are few
+    // instructions, keeps one box copy per stage (slices packed BR rows
+    // apart) and a producer thread that waits for the warps; measured faster
+    // for it.
+    constexpr bool PLANES = MODE != MODE_FAST;
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
+    __shared__ unsigned done[NST];  // warps done with each stage, counted over all its uses
     extern __shared__ __align__(1024) float ring[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
@@ -669,26 +723,35 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
         }
         return;
     }
-    const int plane = BR * PBOX_C;
-    // rows of slice q start at row q * BR of the swizzle pattern: with BR a
-    // multiple of 4, odd slices see the pattern shifted by 4 rows, which is
-    // the chunk index xor 4 (slot xor 16)
-    const int flip = (BR & 4) ? 16 : 0;
+    // PLANES: every slice of a stage has its own 4 KB plane, 1024-byte
+    // aligned, so all slices see the same swizzle phase and a gather's
+    // slices differ by constant offsets.  Otherwise the rows of slice q start
+    // at row q * BR of the swizzle pattern: with BR a multiple of 4, odd
+    // slices see the pattern shifted by 4 rows, which is the chunk index
+    // xor 4 (slot xor 16).
+    const int plane = PLANES ? PLANE : BR * PBOX_C;
+    const int flip = PLANES ? 0 : ((BR & 4) ? 16 : 0);
     // (CT = 0 keeps a single dummy slot: every entry is read from memory)
     int li[CT > 0 ? CT : 1];
-    float w[CT > 0 ? CT : 1], wl[CT > 0 ? CT : 1];
+    float w[CT > 0 ? CT : 1];
     double wd[CT > 0 ? CT : 1];
+    // the compensated mode's weights as packed pairs (wh, wh), (-wh, -wh), (wl, wl)
+    uint64_t fh[CT > 0 ? CT : 1], fhn[CT > 0 ? CT : 1], fl[CT > 0 ? CT : 1];
 #pragma unroll
     for (int k = 0; k < CT; k++) {
         if constexpr (EXACT) {
             li[k] = k < nk ? box_slot_of(col[s + k], org, nd) : 0;
             wd[k] = k < nk ? dval[s + k] : 0.0;
             w[k] = 0.f;
-            wl[k] = 0.f;
+        } else if constexpr (MODE == MODE_FF) {
+            li[k] = k < nk ? (int)slot[s + k] : 0;
+            const float a = k < nk ? bval[s + k] : 0.f, b = k < nk ? blo[s + k] : 0.f;
+            fh[k] = f2_pack(a, a);
+            fhn[k] = f2_pack(-a, -a);
+            fl[k] = f2_pack(b, b);
         } else {
             li[k] = k < nk ? (int)slot[s + k] : 0;
             w[k] = k < nk ? bval[s + k] : 0.f;
-            wl[k] = (MODE == MODE_FF && k < nk) ? blo[s + k] : 0.f;
             wd[k] = 0.0;
         }
     }
@@ -696,14 +759,26 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
         for (int k = 0; k < NST; k++) {
             mbar_init(&full[k], 1);
             mbar_init(&empty[k], PATCH_WARPS);
+            done[k] = 0u;
         }
         asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
     }
     __syncthreads();
     const int64_t ngroups = (d1 - d0 + SPS - 1) / SPS;
+    // PLANES: one box copy per slice of the group (slices past the chunk are
+    // not loaded); else one copy of box_bytes for the whole stage
     auto issue = [&](int st, int64_t grp) {
-        mbar_expect_tx(&full[st], stage_bytes);
-        tma_load_3d(ring + (int64_t)st * stage_floats, &tmap, org.y, org.x, (int)(d0 + grp * SPS), &full[st]);
+        const int64_t z0 = d0 + grp * SPS;
+        if constexpr (PLANES) {
+            const int n = (int)(d1 - z0 < SPS ? d1 - z0 : SPS);
+            mbar_expect_tx(&full[st], (unsigned)n * box_bytes);
+            for (int q = 0; q < n; q++)
+                tma_load_3d(ring + (int64_t)st * stage_floats + q * PLANE, &tmap, org.y, org.x, (int)(z0 + q),
+                            &full[st]);
+        } else {
+            mbar_expect_tx(&full[st], box_bytes);
+            tma_load_3d(ring + (int64_t)st * stage_floats, &tmap, org.y, org.x, (int)z0, &full[st]);
+        }
     };
     if (t == 0)
         for (int k = 0; k < NST && k < ngroups; k++) issue(k, k);
@@ -712,10 +787,12 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
         const unsigned ph = (unsigned)((grp / NST) & 1);
         const bool got = mbar_wait_bounded(&full[st], ph);
         if (!__all_sync(0xffffffffu, got)) {
-            if (lane == 0) atomicOr(flags, FLAG_TIMEOUT);
-            if (t == 0)  // the copies still in flight: bounded wait before leaving
+            if (lane == 0) {
+                atomicOr(flags, FLAG_TIMEOUT);
+                // copies of this block that may still be in flight: bounded wait before leaving
                 for (int64_t q = grp + 1; q < grp + NST && q < ngroups; q++)
                     (void)mbar_wait_bounded(&full[q % NST], (unsigned)((q / NST) & 1));
+            }
             return;
         }
         const float* buf = ring + (int64_t)st * stage_floats;
@@ -747,23 +824,38 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
             }
         } else if constexpr (MODE == MODE_FF) {
             if (o >= 0) {
-                float h[SPS], l[SPS];
+                // slices 2j and 2j + 1 of the stage as one packed pair
+                static_assert(SPS % 2 == 0, "the compensated apply stages slices in pairs");
+                uint64_t h2[SPS / 2], l2[SPS / 2];
 #pragma unroll
-                for (int q = 0; q < SPS; q++) h[q] = l[q] = 0.f;
+                for (int j = 0; j < SPS / 2; j++) h2[j] = l2[j] = 0ull;
 #pragma unroll
                 for (int k = 0; k < CT; k++) {
                     if (k < nk) {
+                        const int a = li[k], b = li[k] ^ flip;
 #pragma unroll
-                        for (int q = 0; q < SPS; q++)
-                            ff_step(h[q], l[q], w[k], wl[k], buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))]);
+                        for (int j = 0; j < SPS / 2; j++)
+                            ff_step2(h2[j], l2[j], fh[k], fhn[k], fl[k],
+                                     f2_pack(buf[2 * j * plane + a], buf[(2 * j + 1) * plane + b]));
                     }
                 }
                 for (int64_t k = s + CT; k < e; k++) {
                     const float wk = bval[k], wlk = blo[k];
-                    const int sk = slot[k];
+                    const uint64_t kh = f2_pack(wk, wk), khn = f2_pack(-wk, -wk), kl = f2_pack(wlk, wlk);
+                    const int a = slot[k], b = a ^ flip;
 #pragma unroll
-                    for (int q = 0; q < SPS; q++)
-                        ff_step(h[q], l[q], wk, wlk, buf[q * plane + (sk ^ ((q & 1) ? flip : 0))]);
+                    for (int j = 0; j < SPS / 2; j++)
+                        ff_step2(h2[j], l2[j], kh, khn, kl,
+                                 f2_pack(buf[2 * j * plane + a], buf[(2 * j + 1) * plane + b]));
+                }
+                float h[SPS], l[SPS];
+#pragma unroll
+                for (int j = 0; j < SPS / 2; j++) {
+                    const float2 hv = f2_unpack(h2[j]), lv = f2_unpack(l2[j]);
+                    h[2 * j] = hv.x;
+                    h[2 * j + 1] = hv.y;
+                    l[2 * j] = lv.x;
+                    l[2 * j + 1] = lv.y;
                 }
 #pragma unroll
                 for (int q = 0; q < SPS; q++) {
@@ -810,18 +902,35 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
             for (int q = 0; q < SPS; q++)
                 if (ds + q < d1) out[(ds + q) * n_out] = acc[q];
         }
+        // The last warp done with the stage refills it, so no warp waits for
+        // the others (the slowest warp, with the longest rows, no longer
+        // holds a producer thread back).  Its lanes' reads of the stage are
+        // ordered before the count (syncwarp, then a release fence); the last
+        // one acquires them all before the async-proxy copy overwrites it.
         __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[st]);  // this warp is done with the stage
-        if (t == 0 && grp + NST < ngroups) {
-            if (!mbar_wait_bounded(&empty[st], ph)) {
-                atomicOr(flags, FLAG_TIMEOUT);
-                for (int64_t q = grp + 1; q < grp + NST && q < ngroups; q++)
-                    (void)mbar_wait_bounded(&full[q % NST], (unsigned)((q / NST) & 1));
-                return;
+        if constexpr (PLANES) {
+            if (lane == 0) {
+                __threadfence_block();
+                const unsigned n = atomicAdd(&done[st], 1u) + 1u;
+                if (n == (unsigned)(grp / NST + 1) * PATCH_WARPS && grp + NST < ngroups) {
+                    __threadfence_block();
+                    asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                    issue(st, grp + NST);
+                }
             }
-            // the warps' generic-proxy reads of the stage before the async-proxy writes
-            asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
-            issue(st, grp + NST);
+        } else {
+            if (lane == 0) mbar_arrive(&empty[st]);  // this warp is done with the stage
+            if (t == 0 && grp + NST < ngroups) {
+                if (!mbar_wait_bounded(&empty[st], ph)) {
+                    atomicOr(flags, FLAG_TIMEOUT);
+                    for (int64_t q = grp + 1; q < grp + NST && q < ngroups; q++)
+                        (void)mbar_wait_bounded(&full[q % NST], (unsigned)((q / NST) & 1));
+                    return;
+                }
+                // the warps' generic-proxy reads of the stage before the async-proxy writes
+                asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory");
+                issue(st, grp + NST);
+            }
         }
     }
 }
@@ -1321,16 +1430,18 @@ constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]
 struct FFConfig {
     int sps, nst, minb, cached;
 };
-constexpr FFConfig kFFConfigs[] = {{4, 2, 0, 8}, {4, 3, 3, 4}, {8, 2, 3, 4}, {4, 3, 3, 0},
-                                   {8, 2, 2, 8}, {2, 4, 4, 0}, {4, 2, 4, 0}};
+constexpr FFConfig kFFConfigs[] = {{4, 2, 0, 8}, {4, 3, 0, 8}, {4, 4, 0, 8}, {8, 2, 0, 8},
+                                   {8, 2, 2, 8}, {4, 3, 3, 4}, {4, 2, 4, 0}};
 constexpr int kNumFFConfigs = (int)(sizeof(kFFConfigs) / sizeof(kFFConfigs[0]));
 
 template <int SPS, int NST, int MINB, int MODE = MODE_FAST, int CT = CACHED_T>
 int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, const float* vin, void* vout,
                  int64_t stack, cudaStream_t s) {
     const int BR = W->box_rows;
-    const int stage_floats = (SPS * BR * PBOX_C + 255) & ~255;  // stages start on 1024-byte boundaries
-    const unsigned stage_bytes = (unsigned)(box_slices * BR * PBOX_C * 4);
+    // stages (and with planes, every slice) start on 1024-byte boundaries
+    constexpr bool PLANES = MODE != MODE_FAST;
+    const int stage_floats = PLANES ? SPS * PLANE : (SPS * BR * PBOX_C + 255) & ~255;
+    const unsigned box_bytes = (unsigned)((PLANES ? 1 : box_slices) * BR * PBOX_C * 4);
     const size_t smem = (size_t)NST * stage_floats * sizeof(float);
     if (smem > 200 * 1024) return RG_ERR_UNSUPPORTED;
     static std::once_flag attr;
@@ -1355,7 +1466,7 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
     apply_patch_tma<SPS, NST, MINB, MODE, CT><<<grid, 32 * PATCH_WARPS, smem, s>>>(
         map, W->row_ptr, W->col, FF ? W->ff_slot : W->box_slot, FF ? W->ff_hi : W->box_val, FF ? W->ff_lo : nullptr,
         W->val32, W->val, OUT64 ? (double*)vout : nullptr, FastDiv((uint32_t)W->in_shape1), patch_grid(W), patches, W->box_origin, BR,
-        stage_floats, stage_bytes, vin, W->n_in, OUT64 ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags,
+        stage_floats, box_bytes, vin, W->n_in, OUT64 ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags,
         OUT64 ? W->box_perm : nullptr);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
@@ -1381,7 +1492,7 @@ int launch_box_config_mode(const rg_weights_s* W, int cfg, const float* vin, voi
     // stage's other slices are never stored)
     const int bs = (int)std::min<int64_t>(c.sps, stack);
     CUtensorMap map;
-    if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
+    if (!encode_stack(W, vin, stack, MODE == MODE_FAST ? bs : 1, &map)) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
         case 0: return launch_patch<4, 2, 0, MODE>(W, map, bs, vin, vout, stack, s);
         case 1: return launch_patch<4, 2, 4, MODE>(W, map, bs, vin, vout, stack, s);
@@ -1398,14 +1509,14 @@ int launch_ff_config(const rg_weights_s* W, int cfg, const float* vin, void* vou
     const FFConfig c = kFFConfigs[cfg];
     const int bs = (int)std::min<int64_t>(c.sps, stack);
     CUtensorMap map;
-    if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
+    if (!encode_stack(W, vin, stack, 1, &map)) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
         case 0: return launch_patch<4, 2, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
-        case 1: return launch_patch<4, 3, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
-        case 2: return launch_patch<8, 2, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
-        case 3: return launch_patch<4, 3, 3, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
+        case 1: return launch_patch<4, 3, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
+        case 2: return launch_patch<4, 4, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
+        case 3: return launch_patch<8, 2, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
         case 4: return launch_patch<8, 2, 2, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
-        case 5: return launch_patch<2, 4, 4, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
+        case 5: return launch_patch<4, 3, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
         case 6: return launch_patch<4, 2, 4, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
     }
     return RG_ERR_UNSUPPORTED;
@@ -1546,7 +1657,7 @@ int apply_box_exact(const rg_weights_s* W, const float* vin, double* vout, int64
     if (W->box_state != 1) return RG_ERR_UNSUPPORTED;
     const int bs = (int)std::min<int64_t>(4, stack);
     CUtensorMap map;
-    if (!encode_stack(W, vin, stack, bs, &map)) return RG_ERR_UNSUPPORTED;
+    if (!encode_stack(W, vin, stack, 1, &map)) return RG_ERR_UNSUPPORTED;
     return launch_patch<4, 2, 0, MODE_EXACT>(W, map, bs, vin, vout, stack, s);
 }
 

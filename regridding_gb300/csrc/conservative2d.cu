@@ -128,6 +128,84 @@ __device__ __forceinline__ bool seg_hit(double x1, double y1, double x2, double 
     return (0 <= t && t < 1) && (0 <= u && u < 1);
 }
 
+// ---------------------------------------------------------------------------
+// Certified float32 filter for the walk's crossing test.  On GB300 the FP64
+// pipe runs 2 lanes per clock per SM (1/64 of FP32), and the 13 FP64
+// operations of each candidate edge's determinants were over half of the
+// walk.  The filter evaluates the same determinants in float32 from
+// coordinates truncated to float32 (from their bits: no FP64 instruction),
+// with a static error bound in the manner of Shewchuk's adaptive predicates
+// (Shewchuk 1997, "Adaptive precision floating-point arithmetic and fast
+// robust geometric predicates"), and answers only where the FP64 result is
+// certain; the walk computes the FP64 determinants of the edge it crosses
+// (its t is needed) and of the rare undecided candidates.
+// ---------------------------------------------------------------------------
+
+// v truncated to float32 from its bits: |v - f| < 2^-23 |v|.  Magnitudes
+// below 2^-126 give 0; magnitudes of 2^128 or more (and inf, NaN) clear ok.
+__device__ __forceinline__ float trunc_float(double v, bool& ok) {
+    const unsigned hi = (unsigned)__double2hiint(v), lo = (unsigned)__double2loint(v);
+    const unsigned ah = hi & 0x7fffffffu;
+    ok = ok && ah < 0x47f00000u;
+    const unsigned f = (hi & 0x80000000u) | ((ah - 0x38000000u) << 3) | (lo >> 29);
+    return ah < 0x38100000u ? 0.f : __uint_as_float(f);
+}
+
+// Where q = fl64(n / d) lies against [0, 1), given float32 values nf, df with
+// |nf - n| <= E and |df - d| <= E: 1 inside, 0 outside, -1 undecided.
+//  * d's sign is certain when |df| > E; with it, nn = nf sgn(d), dn = |df|
+//    bound n sgn(d) in [nn - E, nn + E] and |d| in [dn - E, dn + E].
+//  * q > 0 when nn - E > 0, and q < 0 when nn + E < 0 (then |q| is far above
+//    the smallest double, so it does not round to -0).
+//  * q < 1 - 2^-54, which rounds below 1, when (nn + E) / (dn - E) is at most
+//    1 - 2^-16 (the two float roundings of the sums move that ratio by a
+//    factor of at most (1 + 2^-24) / (1 - 2^-24)); q >= 1, which rounds to
+//    at least 1, when nn - E >= (1 + 2^-16)(dn + E).
+__device__ __forceinline__ int unit_quotient_filter(float nf, float df, float E) {
+    const float dn = fabsf(df);
+    if (!(dn > E)) return -1;
+    const float nn = df < 0.f ? -nf : nf;
+    const float lo = __fsub_rn(nn, E), hi = __fadd_rn(nn, E);
+    if (hi < 0.f) return 0;
+    if (lo >= __fmul_rn(1.0000152587890625f, __fadd_rn(dn, E))) return 0;
+    if (lo > 0.f && hi <= __fmul_rn(0.9999847412109375f, __fsub_rn(dn, E))) return 1;
+    return -1;
+}
+
+// Float32 decision of the crossing test of the walk's inside step (both
+// quotients of seg_hit's determinants in [0, 1)) for segment (x1, y1) ->
+// (x1 - dx12, y1 - dy12) and edge (x3, y3) -> (x4, y4), all truncated images
+// of the doubles the FP64 test uses, m at least their largest magnitude:
+// 1 crossed, 0 not crossed, -1 undecided.
+// Error bound: each float difference is within D = 2^-22 m (1 + 2^-21) +
+// 2^-24 |diff| (1 + 2^-22) of the FP64 difference (two truncations of at
+// most 2^-23 of a coordinate, the float rounding, the FP64 rounding); with
+// S the largest float difference, each float determinant is within
+// 4 D S + 2 D^2 + 2^-22 S^2 (plus terms of order 2^-53 S^2) of the FP64 one.
+// The code takes D = 2^-21 m + 2^-23 S and E = 1.0625 (4 D S + 2 D^2 +
+// 2^-19 S^2): twice to eight times those terms, and 6 % for the float
+// rounding of E itself.  S is kept in [2^-40, 2^40] (no float underflow or
+// overflow in the products); otherwise undecided.
+__device__ __forceinline__ int crossing_filter(float x1, float y1, float dx12, float dy12, float x3, float y3,
+                                               float x4, float y4, float m) {
+    const float x13 = __fsub_rn(x1, x3), y13 = __fsub_rn(y1, y3);
+    const float x34 = __fsub_rn(x3, x4), y34 = __fsub_rn(y3, y4);
+    const float S = fmaxf(fmaxf(fmaxf(fabsf(x13), fabsf(y13)), fmaxf(fabsf(x34), fabsf(y34))),
+                          fmaxf(fabsf(dx12), fabsf(dy12)));
+    if (!(S >= 9.094947e-13f && S <= 1.0995116e12f && m <= 1.0995116e12f)) return -1;  // 2^-40, 2^40
+    const float T = __fsub_rn(__fmul_rn(x13, y34), __fmul_rn(y13, x34));
+    const float U = __fsub_rn(__fmul_rn(dx12, y13), __fmul_rn(dy12, x13));
+    const float D = __fsub_rn(__fmul_rn(dx12, y34), __fmul_rn(dy12, x34));
+    const float dd = __fadd_rn(__fmul_rn(4.76837158e-7f, m), __fmul_rn(1.1920929e-7f, S));  // 2^-21 m + 2^-23 S
+    const float E = __fmul_rn(1.0625f, __fadd_rn(__fadd_rn(__fmul_rn(__fmul_rn(4.f, dd), S), __fmul_rn(__fmul_rn(2.f, dd), dd)),
+                                                 __fmul_rn(__fmul_rn(1.9073486e-6f, S), S)));  // 2^-19
+    const int in_t = unit_quotient_filter(T, D, E);
+    if (in_t == 0) return 0;
+    const int in_u = unit_quotient_filter(-U, D, E);
+    if (in_u == 0) return 0;
+    return (in_t == 1 && in_u == 1) ? 1 : -1;
+}
+
 // contribution of one boundary edge to the extended winding number of
 // point_is_inside_polygon (geometry.py:737-829)
 __device__ __forceinline__ double winding_term(double x, double y, double vx0, double vy0,
@@ -774,6 +852,12 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
             const double dx12 = dsub(x1, p2x), dy12 = dsub(y1, p2y);
             int found = -1;
             double f_tdet = 0.0, f_det = 1.0;
+            // float32 images of the segment for the crossing filter
+            bool seg_ok = true;
+            const float x1f = trunc_float(x1, seg_ok), y1f = trunc_float(y1, seg_ok);
+            const float x2f = trunc_float(p2x, seg_ok), y2f = trunc_float(p2y, seg_ok);
+            const float dx12f = __fsub_rn(x1f, x2f), dy12f = __fsub_rn(y1f, y2f);
+            const float mseg = fmaxf(fmaxf(fabsf(x1f), fabsf(y1f)), fmaxf(fabsf(x2f), fabsf(y2f)));
 #pragma unroll 1
             for (int v = 0; v < 4; v++) {
                 if (v == edge_last) continue;
@@ -783,17 +867,29 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
                 double x4 = st.X(stx + c_vtx_i[v], sty + c_vtx_j[v]);
                 double y4 = st.Y(stx + c_vtx_i[v], sty + c_vtx_j[v]);
                 if (!bboxes_intersect(x1, y1, p2x, p2y, x3, y3, x4, y4)) continue;
+                // 1: crossed, 0: not crossed (both certain), -1: the FP64 test decides
+                int dec = -1;
+                {
+                    bool ok = seg_ok;
+                    const float x3f = trunc_float(x3, ok), y3f = trunc_float(y3, ok);
+                    const float x4f = trunc_float(x4, ok), y4f = trunc_float(y4, ok);
+                    const float m = fmaxf(mseg, fmaxf(fmaxf(fabsf(x3f), fabsf(y3f)), fmaxf(fabsf(x4f), fabsf(y4f))));
+                    if (ok) dec = crossing_filter(x1f, y1f, dx12f, dy12f, x3f, y3f, x4f, y4f, m);
+                }
+                if (dec == 0) continue;
                 const double x13 = dsub(x1, x3), y13 = dsub(y1, y3);
                 const double x34 = dsub(x3, x4), y34 = dsub(y3, y4);
                 const double tdet = dsub(dmul(x13, y34), dmul(y13, x34));
-                const double udet = dsub(dmul(dx12, y13), dmul(dy12, x13));
                 const double det = dsub(dmul(dx12, y34), dmul(dy12, x34));
-                const int in_t = quotient_in_unit(tdet, det);
-                const int in_u = quotient_in_unit(-udet, det);
-                if (in_t == 0 || in_u == 0) continue;
-                if (in_t < 0 || in_u < 0) {
-                    const double t = ddiv(tdet, det), u = ddiv(-udet, det);
-                    if (!((0 <= t && t < 1) && (0 <= u && u < 1))) continue;
+                if (dec < 0) {
+                    const double udet = dsub(dmul(dx12, y13), dmul(dy12, x13));
+                    const int in_t = quotient_in_unit(tdet, det);
+                    const int in_u = quotient_in_unit(-udet, det);
+                    if (in_t == 0 || in_u == 0) continue;
+                    if (in_t < 0 || in_u < 0) {
+                        const double t = ddiv(tdet, det), u = ddiv(-udet, det);
+                        if (!((0 <= t && t < 1) && (0 <= u && u < 1))) continue;
+                    }
                 }
                 found = v;
                 f_tdet = tdet;

@@ -800,6 +800,12 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
             double sminy = fmin(y1, p2y), smaxy = fmax(y1, p2y);
             bool found = false;
             double t_min = INFINITY;
+            // float32 images of the segment for the crossing filter
+            bool seg_ok = true;
+            const float x1f = trunc_float(x1, seg_ok), y1f = trunc_float(y1, seg_ok);
+            const float x2f = trunc_float(p2x, seg_ok), y2f = trunc_float(p2y, seg_ok);
+            const float dx12f = __fsub_rn(x1f, x2f), dy12f = __fsub_rn(y1f, y2f);
+            const float mseg = fmaxf(fmaxf(fabsf(x1f), fabsf(y1f)), fmaxf(fabsf(x2f), fabsf(y2f)));
             int64_t best_order = INT64_MAX;
             int best_code = 0;
             int64_t best_cell = 0;
@@ -816,6 +822,16 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
                         for (int32_t q = s0; q < s1; q++) {
                             int32_t ek = __ldg(B.items + q);
                             const Edge e = S.edges[ek];
+                            if (!bboxes_intersect(x1, y1, p2x, p2y, e.x3, e.y3, e.x4, e.y4)) continue;
+                            {
+                                // most candidate boundary edges are certainly not crossed
+                                bool ok = seg_ok;
+                                const float x3f = trunc_float(e.x3, ok), y3f = trunc_float(e.y3, ok);
+                                const float x4f = trunc_float(e.x4, ok), y4f = trunc_float(e.y4, ok);
+                                const float m = fmaxf(mseg, fmaxf(fmaxf(fabsf(x3f), fabsf(y3f)),
+                                                                  fmaxf(fabsf(x4f), fabsf(y4f))));
+                                if (ok && crossing_filter(x1f, y1f, dx12f, dy12f, x3f, y3f, x4f, y4f, m) == 0) continue;
+                            }
                             double t;
                             if (!seg_hit(x1, y1, p2x, p2y, e.x3, e.y3, e.x4, e.y4, &t)) continue;
                             if (e.cell == edge_last) continue;

@@ -690,6 +690,37 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     // the thread's output: the warp tile layout, or for the exact and
     // compensated applies the patch's outputs by row length (a warp's lanes
     // then run chains of similar length)
+    const int64_t d0 = (int64_t)blockIdx.y * chunk;
+    const int64_t d1 = d0 + chunk < stack ? d0 + chunk : stack;
+    const int2 org = origin[p];
+    const int64_t ngroups = (d1 - d0 + SPS - 1) / SPS;
+    // PLANES: one box copy per slice of the group (slices past the chunk are
+    // not loaded); else one copy of box_bytes for the whole stage
+    auto issue = [&](int st, int64_t grp) {
+        const int64_t z0 = d0 + grp * SPS;
+        if constexpr (PLANES) {
+            const int n = (int)(d1 - z0 < SPS ? d1 - z0 : SPS);
+            mbar_expect_tx(&full[st], (unsigned)n * box_bytes);
+            for (int q = 0; q < n; q++)
+                tma_load_3d(ring + (int64_t)st * stage_floats + q * PLANE, &tmap, org.y, org.x, (int)(z0 + q),
+                            &full[st]);
+        } else {
+            mbar_expect_tx(&full[st], box_bytes);
+            tma_load_3d(ring + (int64_t)st * stage_floats, &tmap, org.y, org.x, (int)z0, &full[st]);
+        }
+    };
+    // the first stages' copies start before the threads fetch their rows, so
+    // that the copies and the row fetches overlap (the barriers are ready for
+    // the other threads after the __syncthreads below)
+    if (org.x >= 0 && t == 0) {
+        for (int k = 0; k < NST; k++) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], PATCH_WARPS);
+            done[k] = 0u;
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+        for (int k = 0; k < NST && k < ngroups; k++) issue(k, k);
+    }
     int pr = 4 * (warp >> 1) + (lane >> 3), pc = 8 * (warp & 1) + (lane & 7);
     if (OUT64 && perm) {
         const int raw = perm[p * (PATCH * PATCH) + t];
@@ -697,8 +728,6 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
         pc = raw % PATCH;
     }
     const int64_t o = patch_cell(P, p, pr, pc);
-    const int64_t d0 = (int64_t)blockIdx.y * chunk;
-    const int64_t d1 = d0 + chunk < stack ? d0 + chunk : stack;
     int64_t s = 0, e = 0;
     if (o >= 0) {
         s = row_ptr[o];
@@ -706,7 +735,6 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     }
     const int nk = (int)(e - s);
     float* out = vout + (o >= 0 ? o : 0);
-    const int2 org = origin[p];
     if (org.x < 0) {
         // no entries (all zeros) or a footprint larger than the box: the whole block
         if (o >= 0) {
@@ -755,33 +783,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
             wd[k] = 0.0;
         }
     }
-    if (t == 0) {
-        for (int k = 0; k < NST; k++) {
-            mbar_init(&full[k], 1);
-            mbar_init(&empty[k], PATCH_WARPS);
-            done[k] = 0u;
-        }
-        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
-    }
     __syncthreads();
-    const int64_t ngroups = (d1 - d0 + SPS - 1) / SPS;
-    // PLANES: one box copy per slice of the group (slices past the chunk are
-    // not loaded); else one copy of box_bytes for the whole stage
-    auto issue = [&](int st, int64_t grp) {
-        const int64_t z0 = d0 + grp * SPS;
-        if constexpr (PLANES) {
-            const int n = (int)(d1 - z0 < SPS ? d1 - z0 : SPS);
-            mbar_expect_tx(&full[st], (unsigned)n * box_bytes);
-            for (int q = 0; q < n; q++)
-                tma_load_3d(ring + (int64_t)st * stage_floats + q * PLANE, &tmap, org.y, org.x, (int)(z0 + q),
-                            &full[st]);
-        } else {
-            mbar_expect_tx(&full[st], box_bytes);
-            tma_load_3d(ring + (int64_t)st * stage_floats, &tmap, org.y, org.x, (int)z0, &full[st]);
-        }
-    };
-    if (t == 0)
-        for (int k = 0; k < NST && k < ngroups; k++) issue(k, k);
     for (int64_t grp = 0; grp < ngroups; grp++) {
         const int st = (int)(grp % NST);
         const unsigned ph = (unsigned)((grp / NST) & 1);

@@ -1186,31 +1186,165 @@ __global__ void __launch_bounds__(64)
 
 // One warp per chunk: move its triples from its slots to their place in the
 // emission order.
-__global__ void chunk_compact_kernel(Batch B, const int64_t* __restrict__ counts,
-                                     const int64_t* __restrict__ offsets, const int32_t* __restrict__ s_in,
-                                     const int32_t* __restrict__ s_out, const double* __restrict__ s_val,
-                                     int32_t* __restrict__ raw_in, int32_t* __restrict__ raw_out,
-                                     double* __restrict__ raw_val) {
-    int lane = threadIdx.x & 31;
-    int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
-    if (g >= B.chunk_base[B.G]) return;
-    const int pg = pair_of(B.chunk_base, B.G, g);
-    const ChunkPlan& C = B.C[pg];
-    // output rows of the batch: the pair's rows follow those of the pairs before it
-    const int32_t ob = (int32_t)B.out_base[pg];
-    int f = family_of_chunk(C, g);
-    int64_t base = C.slot_base[f] + (g - C.chunk_base[f]) * C.cap[f];
-    int64_t n = counts[g], dst = offsets[g];
-    for (int64_t q = lane; q < n; q += 32) {
-        raw_in[dst + q] = s_in[base + q];
-        raw_out[dst + q] = s_out[base + q] + ob;
-        raw_val[dst + q] = s_val[base + q];
-    }
-}
 
 // ---------------------------------------------------------------------------
 // merge (regridding/_weights/_weights_arrays.py:44-73)
 // ---------------------------------------------------------------------------
+
+// ---------------------------------------------------------------------------
+// Output-row ordering of the chunked walk's triples, read straight from the
+// chunks' slots (no compacted copy, no index indirection): chunk g's q-th
+// triple has raw position offsets[g] + q (the order of one sequential walk
+// per line), and it goes to the bucket of its output row with the key
+// (input cell << 32 | raw position), so that ordering each row by key gives
+// the same order as the bucket sort of the compacted triples: by input
+// cell, then by raw position.  One warp per chunk in the counting and
+// scattering passes (a chunk's consecutive triples often share a row, and
+// their lanes add to its counter once), one warp per row in the ranking.
+// ---------------------------------------------------------------------------
+
+__device__ __forceinline__ unsigned warp_row_add(unsigned* counters, int32_t b, bool active) {
+    const unsigned lane = threadIdx.x & 31u;
+    const unsigned key = active ? (unsigned)b : 0xffffffffu;
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const unsigned leader = __ffs(peers) - 1;
+    unsigned base = 0;
+    if (active && lane == leader) base = atomicAdd(&counters[b], (unsigned)__popc(peers));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    return base + __popc(peers & ((1u << lane) - 1u));
+}
+
+__global__ void slot_count_rows(Batch B, const int64_t* __restrict__ counts, const int32_t* __restrict__ s_out,
+                                unsigned* __restrict__ rows) {
+    const int lane = threadIdx.x & 31;
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (g >= B.chunk_base[B.G]) return;  // warp-uniform
+    const int pg = pair_of(B.chunk_base, B.G, g);
+    const ChunkPlan& C = B.C[pg];
+    const int32_t ob = (int32_t)B.out_base[pg];
+    const int f = family_of_chunk(C, g);
+    const int64_t base = C.slot_base[f] + (g - C.chunk_base[f]) * C.cap[f];
+    const int64_t n = counts[g];
+    for (int64_t q0 = 0; q0 < n; q0 += 32) {
+        const int64_t q = q0 + lane;
+        const bool active = q < n;
+        (void)warp_row_add(rows, active ? s_out[base + q] + ob : 0, active);
+    }
+}
+
+__global__ void slot_scatter_rows(Batch B, const int64_t* __restrict__ counts, const int64_t* __restrict__ offsets,
+                                  const int32_t* __restrict__ s_in, const int32_t* __restrict__ s_out,
+                                  const double* __restrict__ s_val, const int64_t* __restrict__ row_start,
+                                  unsigned* __restrict__ cursor, int64_t* __restrict__ tkey,
+                                  double* __restrict__ tval) {
+    const int lane = threadIdx.x & 31;
+    const int64_t g = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5;
+    if (g >= B.chunk_base[B.G]) return;  // warp-uniform
+    const int pg = pair_of(B.chunk_base, B.G, g);
+    const ChunkPlan& C = B.C[pg];
+    const int32_t ob = (int32_t)B.out_base[pg];
+    const int f = family_of_chunk(C, g);
+    const int64_t base = C.slot_base[f] + (g - C.chunk_base[f]) * C.cap[f];
+    const int64_t n = counts[g], raw0 = offsets[g];
+    for (int64_t q0 = 0; q0 < n; q0 += 32) {
+        const int64_t q = q0 + lane;
+        const bool active = q < n;
+        const int32_t b = active ? s_out[base + q] + ob : 0;
+        const unsigned pos = warp_row_add(cursor, b, active);
+        if (active) {
+            const int64_t dst = row_start[b] + pos;
+            tkey[dst] = ((int64_t)s_in[base + q] << 32) | (int64_t)(uint32_t)(raw0 + q);
+            tval[dst] = s_val[base + q];
+        }
+    }
+}
+
+constexpr int ROW_SMALL = 64;  // rows ranked by one warp (two keys per lane)
+
+// One warp per output row of at most ROW_SMALL triples: each triple's rank
+// is the number of keys of its row below its own (keys are unique); the row
+// is written out in that order.  Longer rows are listed for rank_rows_long.
+__global__ void rank_rows(const int64_t* __restrict__ row_start, int64_t nrows, const int64_t* __restrict__ tkey,
+                          const double* __restrict__ tval, int32_t* __restrict__ out_in,
+                          double* __restrict__ out_val, int32_t* __restrict__ long_list,
+                          unsigned* __restrict__ long_count) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t r = (blockIdx.x * (int64_t)blockDim.x + threadIdx.x) >> 5; r < nrows; r += nwarps) {
+        const int64_t s = row_start[r], n = row_start[r + 1] - s;  // warp-uniform
+        if (n > ROW_SMALL) {
+            if (lane == 0) long_list[atomicAdd(long_count, 1u)] = (int32_t)r;
+            continue;
+        }
+        const int64_t k0 = lane < n ? tkey[s + lane] : INT64_MAX;
+        const int64_t k1 = lane + 32 < n ? tkey[s + 32 + lane] : INT64_MAX;
+        int r0 = 0, r1 = 0;
+        const int n0 = n < 32 ? (int)n : 32;
+        for (int j = 0; j < n0; j++) {
+            const int64_t kj = __shfl_sync(0xffffffffu, k0, j);
+            r0 += kj < k0;
+            r1 += kj < k1;
+        }
+        for (int j = 32; j < n; j++) {
+            const int64_t kj = __shfl_sync(0xffffffffu, k1, j - 32);
+            r0 += kj < k0;
+            r1 += kj < k1;
+        }
+        if (lane < n) {
+            out_in[s + r0] = (int32_t)(k0 >> 32);
+            out_val[s + r0] = tval[s + lane];
+        }
+        if (lane + 32 < n) {
+            out_in[s + r1] = (int32_t)(k1 >> 32);
+            out_val[s + r1] = tval[s + 32 + lane];
+        }
+    }
+}
+
+// One block per listed long row: keys staged in shared-memory tiles, every
+// thread ranks up to 8 triples per pass.
+constexpr int ROW_TILE = 2048;
+__global__ void __launch_bounds__(256)
+    rank_rows_long(const int64_t* __restrict__ row_start, const int32_t* __restrict__ long_list,
+                   const unsigned* __restrict__ long_count, const int64_t* __restrict__ tkey,
+                   const double* __restrict__ tval, int32_t* __restrict__ out_in, double* __restrict__ out_val) {
+    __shared__ int64_t tile[ROW_TILE];
+    const unsigned nl = *long_count;
+    for (unsigned li = blockIdx.x; li < nl; li += gridDim.x) {
+        const int32_t r = long_list[li];
+        const int64_t s = row_start[r], t = row_start[r + 1], len = t - s;
+        for (int64_t e0 = s; e0 < t; e0 += (int64_t)blockDim.x * 8) {
+            int64_t mykey[8];
+            int64_t rank[8];
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int64_t e = e0 + threadIdx.x + (int64_t)k * blockDim.x;
+                mykey[k] = e < t ? tkey[e] : INT64_MAX;
+                rank[k] = 0;
+            }
+            for (int64_t q0 = 0; q0 < len; q0 += ROW_TILE) {
+                const int64_t m = len - q0 < ROW_TILE ? len - q0 : ROW_TILE;
+                __syncthreads();
+                for (int64_t q = threadIdx.x; q < m; q += blockDim.x) tile[q] = tkey[s + q0 + q];
+                __syncthreads();
+                for (int64_t q = 0; q < m; q++) {
+                    const int64_t kq = tile[q];
+#pragma unroll
+                    for (int k = 0; k < 8; k++) rank[k] += kq < mykey[k];
+                }
+            }
+#pragma unroll
+            for (int k = 0; k < 8; k++) {
+                const int64_t e = e0 + threadIdx.x + (int64_t)k * blockDim.x;
+                if (e < t) {
+                    out_in[s + rank[k]] = (int32_t)(mykey[k] >> 32);
+                    out_val[s + rank[k]] = tval[e];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
 
 __global__ void make_keys(const int32_t* raw_in, int64_t n, int64_t* skey) {
     for (int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; k < n;
@@ -1478,13 +1612,24 @@ int sweep_lines(const Batch& B, int64_t lines, const Seat* seats, int64_t* total
     return st;
 }
 
-// Chunked walk over all lines of the batch (see chunk_walk_kernel).  Sets
-// *nraw_out to -1 (and frees everything) when a chunk needed more slots than
-// it was given or the slots would not fit; fl receives every grid's error word.
+// The triples ordered by output row straight from the chunks' slots
+// (slot_count_rows, slot_scatter_rows, rank_rows): row_start[n_rows + 1] and
+// the rows' input cells and values.
+struct SortedRows {
+    int64_t n_rows = 0;
+    int64_t* row_start = nullptr;
+    int32_t* in = nullptr;
+    double* val = nullptr;
+};
+
+// Chunked walk over all lines of the batch (see chunk_walk_kernel), its
+// triples left in output-row order in *rows.  Sets *nraw_out to -1 (and
+// frees everything) when a chunk needed more slots than it was given or the
+// slots would not fit; fl receives every grid's error word.
+
 int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector<double>& bbox_h,
-                  const Seat* seats, int64_t lines, int64_t* total_dev, cudaStream_t s, int32_t** raw_in,
-                  int32_t** raw_out, double** raw_val, int64_t* nraw_out, std::vector<unsigned>& fl,
-                  ChunkPlan** plans_dev, int64_t** chunk_base_dev) {
+                  const Seat* seats, int64_t lines, int64_t* total_dev, cudaStream_t s, int64_t* nraw_out,
+                  std::vector<unsigned>& fl, ChunkPlan** plans_dev, int64_t** chunk_base_dev, SortedRows* rows) {
     const int G = B.G;
     // sweep segments per chunk: rg_set_sweep_chunk (default 32), the
     // RG_SWEEP_CHUNK environment variable overriding it (0 walks whole lines)
@@ -1591,11 +1736,42 @@ int sweep_chunked(Batch& B, const std::vector<SweepParams>& P, const std::vector
             st = RG_ERR_UNSUPPORTED;
             break;
         }
-        if ((st = dalloc(raw_in, (size_t)nraw, s))) break;
-        if ((st = dalloc(raw_out, (size_t)nraw, s))) break;
-        if ((st = dalloc(raw_val, (size_t)nraw, s))) break;
-        chunk_compact_kernel<<<grid_for(chunks * 32, 256), 256, 0, s>>>(B, counts, offsets, s_in, s_out, s_val,
-                                                                        *raw_in, *raw_out, *raw_val);
+        {
+            // order the triples by output row from the slots
+            const int64_t nr = rows->n_rows;
+            unsigned *rowc = nullptr, *long_count = nullptr;
+            int64_t* tkey = nullptr;
+            double* tval = nullptr;
+            int32_t* long_list = nullptr;
+            do {
+                if ((st = dalloc(&rows->row_start, (size_t)nr + 1, s))) break;
+                if ((st = dalloc(&rows->in, (size_t)std::max<int64_t>(nraw, 1), s))) break;
+                if ((st = dalloc(&rows->val, (size_t)std::max<int64_t>(nraw, 1), s))) break;
+                if ((st = dalloc(&rowc, (size_t)nr + 1, s))) break;
+                if ((st = dalloc(&long_count, 1, s))) break;
+                if ((st = dalloc(&long_list, (size_t)std::max<int64_t>(nr, 1), s))) break;
+                if ((st = dalloc(&tkey, (size_t)std::max<int64_t>(nraw, 1), s))) break;
+                if ((st = dalloc(&tval, (size_t)std::max<int64_t>(nraw, 1), s))) break;
+                zero_async(rowc, sizeof(unsigned) * (nr + 1), s);
+                zero_async(long_count, sizeof(unsigned), s);
+                slot_count_rows<<<grid_for(chunks * 32, 256), 256, 0, s>>>(B, counts, s_out, rowc);
+                if ((st = exclusive_scan_u32_to_i64(rowc, rows->row_start, nr + 1, nullptr, s))) break;
+                zero_async(rowc, sizeof(unsigned) * (nr + 1), s);
+                slot_scatter_rows<<<grid_for(chunks * 32, 256), 256, 0, s>>>(B, counts, offsets, s_in, s_out, s_val,
+                                                                           rows->row_start, rowc, tkey, tval);
+                const unsigned gr = grid_for(nr * 32, 256) > 16384 ? 16384 : grid_for(nr * 32, 256);
+                rank_rows<<<gr, 256, 0, s>>>(rows->row_start, nr, tkey, tval, rows->in, rows->val, long_list,
+                                             long_count);
+                rank_rows_long<<<1024, 256, 0, s>>>(rows->row_start, long_list, long_count, tkey, tval, rows->in,
+                                                    rows->val);
+            } while (0);
+            dfree(rowc, s);
+            dfree(long_count, s);
+            dfree(long_list, s);
+            dfree(tkey, s);
+            dfree(tval, s);
+            if (st) break;
+        }
         e = cudaGetLastError();
         if (e != cudaSuccess) {
             set_error("conservative sweep (compaction): %s", cudaGetErrorString(e));
@@ -1841,36 +2017,45 @@ int build_batch(const PairSpec* pairs, int G, cudaStream_t s, rg_weights_s** W, 
         seat_kernel<<<grid_for(lines * 32, 128), 128, 0, s>>>(B, seats);
         std::vector<unsigned> fl((size_t)G, 0u);
         int64_t nraw = 0;
-        if ((st = sweep_chunked(B, P, bbox_h, seats, lines, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw, fl,
-                                &plans_dev, &chunk_base_dev)))
-            break;
+        SortedRows rows;
+        rows.n_rows = n_out_all;
+        st = sweep_chunked(B, P, bbox_h, seats, lines, total_dev, s, &nraw, fl, &plans_dev, &chunk_base_dev,
+                           &rows);
+        bucket_ptr = rows.row_start;
+        sorted_in = rows.in;
+        sorted_val = rows.val;
+        if (st) break;
         if (nraw < 0) {
             // a chunk overflowed its slots: walk whole lines instead
             if ((st = sweep_lines(B, lines, seats, total_dev, s, &raw_in, &raw_out, &raw_val, &nraw, fl))) break;
         }
         for (int g = 0; g < G; g++) status[g] = walk_status(fl[g]);
 
-        // merge: one bucket sort over the output rows of the whole batch
-        // (sync 4 for the entry count; the per-grid sizes come with it)
-        if ((st = dalloc(&skey, (size_t)nraw, s))) break;
-        if ((st = dalloc(&bucket_ptr, (size_t)n_out_all + 1, s))) break;
-        if ((st = dalloc(&perm, (size_t)nraw, s))) break;
-        if (nraw > 0)
-            make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(raw_in, nraw, skey);
-        // the sort also lays the entries' input indices and values out in
-        // sorted order, so the merge reads them contiguously
-        if ((st = dalloc(&sorted_in, (size_t)nraw, s))) break;
-        if ((st = dalloc(&sorted_val, (size_t)nraw, s))) break;
-        if ((st = bucket_sort(raw_out, skey, nraw, n_out_all, bucket_ptr, perm, flags, s, raw_val, sorted_in,
-                              sorted_val)))
-            break;
-        dfree(skey, s);
-        skey = nullptr;
-        dfree(raw_in, s);
-        dfree(raw_out, s);
-        dfree(raw_val, s);
-        raw_in = raw_out = nullptr;
-        raw_val = nullptr;
+        // merge: the triples in output-row order (sync 4 for the entry count;
+        // the per-grid sizes come with it).  The chunked walk orders them from
+        // its slots; otherwise one bucket sort over the output rows of the
+        // whole batch, which also lays the entries' input indices and values
+        // out in sorted order, so the merge reads them contiguously.
+        if (bucket_ptr == nullptr) {
+            if ((st = dalloc(&skey, (size_t)nraw, s))) break;
+            if ((st = dalloc(&bucket_ptr, (size_t)n_out_all + 1, s))) break;
+            if ((st = dalloc(&perm, (size_t)nraw, s))) break;
+            if (nraw > 0)
+                make_keys<<<grid_for(nraw, 256) > 8192 ? 8192 : grid_for(nraw, 256), 256, 0, s>>>(raw_in, nraw,
+                                                                                                   skey);
+            if ((st = dalloc(&sorted_in, (size_t)nraw, s))) break;
+            if ((st = dalloc(&sorted_val, (size_t)nraw, s))) break;
+            if ((st = bucket_sort(raw_out, skey, nraw, n_out_all, bucket_ptr, perm, flags, s, raw_val, sorted_in,
+                                  sorted_val)))
+                break;
+            dfree(skey, s);
+            skey = nullptr;
+            dfree(raw_in, s);
+            dfree(raw_out, s);
+            dfree(raw_val, s);
+            raw_in = raw_out = nullptr;
+            raw_val = nullptr;
+        }
         if ((st = dalloc(&tmp_col, (size_t)nraw, s))) break;
         if ((st = dalloc(&tmp_val, (size_t)nraw, s))) break;
         if ((st = dalloc(&row_nnz, (size_t)n_out_all + 1, s))) break;

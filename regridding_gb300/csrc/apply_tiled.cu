@@ -36,6 +36,7 @@ constexpr int WARPS = 8;        // warp tiles per block
 constexpr int TR = 4, TC = 8;   // warp tile: TR output rows x TC output columns
 constexpr int PREP_MAX = 1024;  // entries of one warp tile sorted in shared memory (4 KB per warp)
 constexpr int CACHED_T = 8;     // row entries kept in registers across slices
+constexpr int FF_EXTRA = 3;     // compensated mode: further row entries kept in shared memory
 constexpr int SLICES = 4;       // stack slices staged per step
 
 struct TileShape {
@@ -684,6 +685,14 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     constexpr bool PLANES = MODE != MODE_FAST;
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
     __shared__ unsigned done[NST];  // warps done with each stage, counted over all its uses
+    // the compensated mode's entries CT .. CT + FF_EXTRA - 1 of every thread's
+    // row, read once per patch (rows one or two entries longer than the
+    // registers hold are common; reading those entries from global memory at
+    // every stage held back the warp with the longest rows, and with it the
+    // stage's refill)
+    constexpr int NX = (MODE == MODE_FF && CT > 0) ? FF_EXTRA : 1;
+    __shared__ uint16_t ex_slot[NX][32 * PATCH_WARPS];
+    __shared__ float ex_hi[NX][32 * PATCH_WARPS], ex_lo[NX][32 * PATCH_WARPS];
     extern __shared__ __align__(1024) float ring[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
@@ -783,6 +792,15 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
             wd[k] = 0.0;
         }
     }
+    if constexpr (MODE == MODE_FF && CT > 0) {
+#pragma unroll
+        for (int j = 0; j < NX; j++) {
+            const bool has = CT + j < nk;
+            ex_slot[j][t] = has ? slot[s + CT + j] : (uint16_t)0;
+            ex_hi[j][t] = has ? bval[s + CT + j] : 0.f;
+            ex_lo[j][t] = has ? blo[s + CT + j] : 0.f;
+        }
+    }
     __syncthreads();
     for (int64_t grp = 0; grp < ngroups; grp++) {
         const int st = (int)(grp % NST);
@@ -841,7 +859,21 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                                      f2_pack(buf[2 * j * plane + a], buf[(2 * j + 1) * plane + b]));
                     }
                 }
-                for (int64_t k = s + CT; k < e; k++) {
+                if constexpr (CT > 0) {
+#pragma unroll
+                    for (int j = 0; j < NX; j++) {
+                        if (CT + j < nk) {
+                            const float wk = ex_hi[j][t], wlk = ex_lo[j][t];
+                            const uint64_t kh = f2_pack(wk, wk), khn = f2_pack(-wk, -wk), kl = f2_pack(wlk, wlk);
+                            const int a = ex_slot[j][t], b = a ^ flip;
+#pragma unroll
+                            for (int q = 0; q < SPS / 2; q++)
+                                ff_step2(h2[q], l2[q], kh, khn, kl,
+                                         f2_pack(buf[2 * q * plane + a], buf[(2 * q + 1) * plane + b]));
+                        }
+                    }
+                }
+                for (int64_t k = s + (CT > 0 ? CT + NX : 0); k < e; k++) {
                     const float wk = bval[k], wlk = blo[k];
                     const uint64_t kh = f2_pack(wk, wk), khn = f2_pack(-wk, -wk), kl = f2_pack(wlk, wlk);
                     const int a = slot[k], b = a ^ flip;
@@ -1432,8 +1464,8 @@ constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]
 struct FFConfig {
     int sps, nst, minb, cached;
 };
-constexpr FFConfig kFFConfigs[] = {{4, 2, 0, 8}, {4, 3, 0, 8}, {4, 4, 0, 8}, {8, 2, 0, 8},
-                                   {8, 2, 2, 8}, {4, 3, 3, 4}, {4, 2, 4, 0}};
+constexpr FFConfig kFFConfigs[] = {{4, 2, 0, 6}, {4, 2, 0, 7}, {4, 3, 0, 6}, {8, 2, 0, 6},
+                                   {2, 4, 0, 6}, {4, 3, 3, 4}, {4, 2, 4, 0}};
 constexpr int kNumFFConfigs = (int)(sizeof(kFFConfigs) / sizeof(kFFConfigs[0]));
 
 template <int SPS, int NST, int MINB, int MODE = MODE_FAST, int CT = CACHED_T>
@@ -1513,11 +1545,11 @@ int launch_ff_config(const rg_weights_s* W, int cfg, const float* vin, void* vou
     CUtensorMap map;
     if (!encode_stack(W, vin, stack, 1, &map)) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
-        case 0: return launch_patch<4, 2, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
-        case 1: return launch_patch<4, 3, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
-        case 2: return launch_patch<4, 4, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
-        case 3: return launch_patch<8, 2, 0, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
-        case 4: return launch_patch<8, 2, 2, MODE_FF, 8>(W, map, bs, vin, vout, stack, s);
+        case 0: return launch_patch<4, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 1: return launch_patch<4, 2, 0, MODE_FF, 7>(W, map, bs, vin, vout, stack, s);
+        case 2: return launch_patch<4, 3, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 3: return launch_patch<8, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 4: return launch_patch<2, 4, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
         case 5: return launch_patch<4, 3, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
         case 6: return launch_patch<4, 2, 4, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);
     }

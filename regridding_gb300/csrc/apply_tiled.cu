@@ -37,6 +37,7 @@ constexpr int TR = 4, TC = 8;   // warp tile: TR output rows x TC output columns
 constexpr int PREP_MAX = 1024;  // entries of one warp tile sorted in shared memory (4 KB per warp)
 constexpr int CACHED_T = 8;     // row entries kept in registers across slices
 constexpr int FF_EXTRA = 3;     // compensated mode: further row entries kept in shared memory
+constexpr int ROW_EXTRA = 2;    // fast and exact modes: further row entries kept in shared memory
 constexpr int SLICES = 4;       // stack slices staged per step
 
 struct TileShape {
@@ -685,14 +686,18 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
     constexpr bool PLANES = MODE != MODE_FAST;
     __shared__ __align__(8) uint64_t full[NST], empty[NST];
     __shared__ unsigned done[NST];  // warps done with each stage, counted over all its uses
-    // the compensated mode's entries CT .. CT + FF_EXTRA - 1 of every thread's
-    // row, read once per patch (rows one or two entries longer than the
-    // registers hold are common; reading those entries from global memory at
-    // every stage held back the warp with the longest rows, and with it the
-    // stage's refill)
-    constexpr int NX = (MODE == MODE_FF && CT > 0) ? FF_EXTRA : 1;
+    // entries CT .. CT + NX - 1 of every thread's row, read once per patch
+    // (rows one or two entries longer than the registers hold are common;
+    // reading those entries from global memory at every stage held back the
+    // warp with the longest rows, and with it the stage's refill): their
+    // slots, and their float32 weights (fast), float32 weight and rest
+    // (compensated) or float64 weights (exact)
+    constexpr int NX = CT > 0 ? (MODE == MODE_FF ? FF_EXTRA : ROW_EXTRA) : 1;
+    constexpr int NXF = MODE != MODE_EXACT ? NX : 1, NXL = MODE == MODE_FF ? NX : 1;
+    constexpr int NXD = MODE == MODE_EXACT ? NX : 1;
     __shared__ uint16_t ex_slot[NX][32 * PATCH_WARPS];
-    __shared__ float ex_hi[NX][32 * PATCH_WARPS], ex_lo[NX][32 * PATCH_WARPS];
+    __shared__ float ex_hi[NXF][32 * PATCH_WARPS], ex_lo[NXL][32 * PATCH_WARPS];
+    __shared__ double ex_d[NXD][32 * PATCH_WARPS];
     extern __shared__ __align__(1024) float ring[];
     const int t = threadIdx.x, warp = t >> 5, lane = t & 31;
     const int64_t p = blockIdx.x;
@@ -792,13 +797,18 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
             wd[k] = 0.0;
         }
     }
-    if constexpr (MODE == MODE_FF && CT > 0) {
+    if constexpr (CT > 0) {
 #pragma unroll
         for (int j = 0; j < NX; j++) {
             const bool has = CT + j < nk;
-            ex_slot[j][t] = has ? slot[s + CT + j] : (uint16_t)0;
-            ex_hi[j][t] = has ? bval[s + CT + j] : 0.f;
-            ex_lo[j][t] = has ? blo[s + CT + j] : 0.f;
+            if constexpr (EXACT) {
+                ex_slot[j][t] = has ? (uint16_t)box_slot_of(col[s + CT + j], org, nd) : (uint16_t)0;
+                ex_d[j][t] = has ? dval[s + CT + j] : 0.0;
+            } else {
+                ex_slot[j][t] = has ? slot[s + CT + j] : (uint16_t)0;
+                ex_hi[j][t] = has ? bval[s + CT + j] : 0.f;
+                if constexpr (MODE == MODE_FF) ex_lo[j][t] = has ? blo[s + CT + j] : 0.f;
+            }
         }
     }
     __syncthreads();
@@ -831,7 +841,20 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                                 acc[q], __dmul_rn(wd[k], widen(buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))])));
                     }
                 }
-                for (int64_t k = s + CT; k < e; k++) {
+                if constexpr (CT > 0) {
+#pragma unroll
+                    for (int j = 0; j < NX; j++) {
+                        if (CT + j < nk) {
+                            const double wk = ex_d[j][t];
+                            const int sk = ex_slot[j][t];
+#pragma unroll
+                            for (int q = 0; q < SPS; q++)
+                                acc[q] = __dadd_rn(acc[q],
+                                                   __dmul_rn(wk, widen(buf[q * plane + (sk ^ ((q & 1) ? flip : 0))])));
+                        }
+                    }
+                }
+                for (int64_t k = s + (CT > 0 ? CT + NX : 0); k < e; k++) {
                     const double wk = dval[k];
                     const int sk = box_slot_of(col[k], org, nd);
 #pragma unroll
@@ -926,7 +949,19 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                         acc[q] = fmaf(w[k], buf[q * plane + (li[k] ^ ((q & 1) ? flip : 0))], acc[q]);
                 }
             }
-            for (int64_t k = s + CT; k < e; k++) {
+            if constexpr (CT > 0) {
+#pragma unroll
+                for (int j = 0; j < NX; j++) {
+                    if (CT + j < nk) {
+                        const float wk = ex_hi[j][t];
+                        const int sk = ex_slot[j][t];
+#pragma unroll
+                        for (int q = 0; q < SPS; q++)
+                            acc[q] = fmaf(wk, buf[q * plane + (sk ^ ((q & 1) ? flip : 0))], acc[q]);
+                    }
+                }
+            }
+            for (int64_t k = s + (CT > 0 ? CT + NX : 0); k < e; k++) {
                 const float wk = bval[k];
                 const int sk = slot[k];
 #pragma unroll

@@ -545,19 +545,22 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS)
     }
 }
 
-// Per patch, the threads' outputs for the exact apply: the patch's cells
-// sorted by row length, longest first (ties by cell), so the 32 lanes of a
-// warp run float64 chains of similar length.  A bitonic sort of 256 keys in
-// shared memory; one block per patch.
+// Per patch, the threads' outputs for the exact and compensated applies: the
+// patch's cells sorted by row length, longest first, so the 32 lanes of a
+// warp run chains of similar length.  Lengths are compared in classes of
+// `group` (1: exact lengths; the compensated apply takes classes of 3, which
+// keeps more of a warp's cells near each other, so that more lanes share
+// input words, for a little more divergence); ties by cell.  A bitonic sort
+// of 256 keys in shared memory; one block per patch.
 __global__ void __launch_bounds__(PATCH * PATCH)
-    perm_patch(const int64_t* __restrict__ row_ptr, PatchGrid P, uint8_t* __restrict__ perm) {
+    perm_patch(const int64_t* __restrict__ row_ptr, PatchGrid P, int group, uint8_t* __restrict__ perm) {
     __shared__ unsigned key[PATCH * PATCH];
     const int t = threadIdx.x;
     const int64_t p = blockIdx.x;
     const int64_t o = patch_cell(P, p, t / PATCH, t % PATCH);
     int64_t nk = o >= 0 ? row_ptr[o + 1] - row_ptr[o] : 0;
     if (nk > 255) nk = 255;
-    key[t] = ((unsigned)(255 - nk) << 8) | (unsigned)t;
+    key[t] = ((unsigned)((255 - nk) / group) << 8) | (unsigned)t;
     __syncthreads();
     for (int k = 2; k <= PATCH * PATCH; k <<= 1) {
         for (int j = k >> 1; j > 0; j >>= 1) {
@@ -1382,18 +1385,30 @@ int box_perm_for(rg_weights_s* W, cudaStream_t s, bool* made) {
     if (W->box_perm || W->box_state != 1) return RG_OK;
     *made = true;
     RG_TRY(dalloc(&W->box_perm, (size_t)W->box_patches * PATCH * PATCH, s));
-    perm_patch<<<(unsigned)W->box_patches, PATCH * PATCH, 0, s>>>(W->row_ptr, patch_grid(W), W->box_perm);
+    perm_patch<<<(unsigned)W->box_patches, PATCH * PATCH, 0, s>>>(W->row_ptr, patch_grid(W), 1, W->box_perm);
+    RG_CUDA(cudaGetLastError());
+    return RG_OK;
+}
+
+// The compensated apply's per-patch thread order (row lengths in classes of 3).
+constexpr int FF_LENGTH_CLASS = 3;
+int ff_perm_for(rg_weights_s* W, cudaStream_t s, bool* made) {
+    if (W->ff_perm || W->box_state != 1) return RG_OK;
+    *made = true;
+    RG_TRY(dalloc(&W->ff_perm, (size_t)W->box_patches * PATCH * PATCH, s));
+    perm_patch<<<(unsigned)W->box_patches, PATCH * PATCH, 0, s>>>(W->row_ptr, patch_grid(W), FF_LENGTH_CLASS,
+                                                                  W->ff_perm);
     RG_CUDA(cudaGetLastError());
     return RG_OK;
 }
 
 // The compensated apply's entry order (made once, after the box lists):
-// threads take the patch's outputs by row length (box_perm), and every
+// threads take the patch's outputs by row length (ff_perm), and every
 // lane's entries are ordered for that layout with their float32 weights and
 // the weights' float32 rests.
 int ff_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
     if (W->ff_slot || W->box_state != 1) return RG_OK;
-    RG_TRY(box_perm_for(W, s, made));
+    RG_TRY(ff_perm_for(W, s, made));
     *made = true;
     int st = RG_OK;
     do {
@@ -1401,7 +1416,7 @@ int ff_lists_for(rg_weights_s* W, cudaStream_t s, bool* made) {
         if ((st = dalloc(&W->ff_hi, (size_t)W->nnz, s))) break;
         if ((st = dalloc(&W->ff_lo, (size_t)W->nnz, s))) break;
         order_patch<<<(unsigned)W->box_patches, 32 * PATCH_WARPS, 0, s>>>(
-            W->row_ptr, W->col, FastDiv((uint32_t)W->in_shape1), W->val32, W->val, patch_grid(W), W->box_origin, W->box_perm, nullptr,
+            W->row_ptr, W->col, FastDiv((uint32_t)W->in_shape1), W->val32, W->val, patch_grid(W), W->box_origin, W->ff_perm, nullptr,
             W->ff_slot, W->ff_hi, W->ff_lo);
         if (cudaGetLastError() != cudaSuccess) {
             set_error("apply (compensated lists): launch failed");
@@ -1536,7 +1551,7 @@ int launch_patch(const rg_weights_s* W, const CUtensorMap& map, int box_slices, 
         map, W->row_ptr, W->col, FF ? W->ff_slot : W->box_slot, FF ? W->ff_hi : W->box_val, FF ? W->ff_lo : nullptr,
         W->val32, W->val, OUT64 ? (double*)vout : nullptr, FastDiv((uint32_t)W->in_shape1), patch_grid(W), patches, W->box_origin, BR,
         stage_floats, box_bytes, vin, W->n_in, OUT64 ? nullptr : (float*)vout, W->n_out, stack, chunk, W->dflags,
-        OUT64 ? W->box_perm : nullptr);
+        FF ? W->ff_perm : (OUT64 ? W->box_perm : nullptr));
     RG_CUDA(cudaGetLastError());
     return RG_OK;
 }
@@ -1708,7 +1723,7 @@ int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stac
 
 // The compensated (float-float) TMA apply with its tuned configuration.
 int apply_box_ff(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s) {
-    if (W->box_state != 1 || W->box_cfg_ff < 0 || !W->ff_slot || !W->box_perm) return RG_ERR_UNSUPPORTED;
+    if (W->box_state != 1 || W->box_cfg_ff < 0 || !W->ff_slot || !W->ff_perm) return RG_ERR_UNSUPPORTED;
     return launch_box_config(W, MODE_FF, W->box_cfg_ff, vin, vout, stack, s);
 }
 

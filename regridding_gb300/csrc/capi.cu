@@ -161,6 +161,7 @@ void free_weights(rg_weights_s* W, cudaStream_t s) {
     dfree(W->ff_hi, s);
     dfree(W->ff_lo, s);
     dfree(W->box_perm, s);
+    dfree(W->ff_perm, s);
     dfree(W->dflags, s);
     delete W;
 }
@@ -634,6 +635,7 @@ int rg_weights_device_bytes(rg_weights w, int64_t* bytes) {
     if (w->box_state == 1) b += w->box_patches * 8 + nnz * 6;  // origins; slot and float32 weight per entry
     if (w->ff_slot) b += nnz * 10;                              // compensated: slot, hi and lo per entry
     if (w->box_perm) b += w->box_patches * 256;
+    if (w->ff_perm) b += w->box_patches * 256;
     *bytes = b;
     return RG_OK;
 }

@@ -233,7 +233,8 @@ struct rg_weights_s {
     float* box_val = nullptr;      // float32 weights in that order
     // the compensated (float-float) apply: per entry its box slot, float32
     // weight hi = (float)w and rest lo = (float)(w - hi), in the order its
-    // row-length thread layout (box_perm) gathers them; its tuned configuration
+    // row-length thread layout (ff_perm) gathers them; its tuned configuration
+    uint8_t* ff_perm = nullptr;    // compensated apply: per patch, thread -> output (row-length classes)
     uint16_t* ff_slot = nullptr;
     float* ff_hi = nullptr;
     float* ff_lo = nullptr;

@@ -416,8 +416,29 @@ class GpuBackend:
         with self._range("serve.apply"):
             self._run(slot, weights, requests, staged)
 
+    # a request whose stack in host memory is at least this large is applied
+    # by rg_apply_host: chunks of ~128 MB are copied in, applied and copied
+    # out on three streams, so the two copy directions and the kernels overlap
+    PIPELINE_BYTES = 192 << 20
+
+    def _pipelined(self, requests: list, staged) -> bool:
+        if staged is not None or len(requests) != 1:
+            return False
+        r = requests[0]
+        v, o = r.values, r.out
+        return (v.device.type == "cpu" and o.device.type == "cpu" and v.is_contiguous() and o.is_contiguous()
+                and v.is_pinned() and o.is_pinned() and v.numel() * v.element_size() >= self.PIPELINE_BYTES)
+
     def _run(self, slot, weights, requests: list, staged=None) -> None:
         t = self.torch
+        if self._pipelined(requests, staged):
+            r = requests[0]
+            dt = {t.float32: _lib.RG_F32, t.float64: _lib.RG_F64}
+            _lib.call("rg_apply_host", weights.handle, ctypes.c_void_p(r.values.data_ptr()), dt[r.values.dtype],
+                      ctypes.c_void_p(r.out.data_ptr()), dt[r.out.dtype], int(r.stack), _lib.RG_ACC[self.accumulate],
+                      0, ctypes.c_void_p(slot.stream.cuda_stream))
+            slot.stream.synchronize()
+            return
         with t.cuda.stream(slot.stream):
             if staged is not None:
                 vin, done = staged
@@ -513,7 +534,12 @@ class RegridServer:
         self.max_batch_stack = int(max_batch_stack)
         self.max_cobuild = int(max_cobuild) if hasattr(self.backend, "build_many") else 0
         self.cobuild_max_cells = int(cobuild_max_cells)
-        self._cv = threading.Condition()
+        # one lock; the scheduler waits on _cv, each slot's worker on its own
+        # condition, so that a state change wakes only the thread it concerns
+        # (waking all 17 threads on every change cost host time under load)
+        lock = threading.RLock()
+        self._cv = threading.Condition(lock)
+        self._slot_cv = [threading.Condition(lock) for _ in range(slots)]
         self._pending: collections.deque[_Request] = collections.deque()
         self._building: set = set()
         self._transient = 0  # footprints of admitted jobs
@@ -561,7 +587,7 @@ class RegridServer:
                 return fut
             if key is not None:
                 self._pending.append(req)
-                self._cv.notify_all()
+                self._cv.notify()
                 return fut
             self._intake_n += 1
         # hashing the grids (native, GIL released) runs on the intake pool so
@@ -577,12 +603,12 @@ class RegridServer:
             req.future.set_exception(e)
             with self._cv:
                 self._intake_n -= 1
-                self._cv.notify_all()
+                self._cv.notify()
             return
         with self._cv:
             self._intake_n -= 1
             self._pending.append(req)
-            self._cv.notify_all()
+            self._cv.notify()
 
     def close(self, wait: bool = True) -> None:
         """Stop accepting requests; finish what is queued when wait, else fail it."""
@@ -596,10 +622,10 @@ class RegridServer:
                 while self._pending:
                     self._pending.popleft().future.set_exception(RuntimeError("server closed"))
             self._running = False
-            self._cv.notify_all()
+            self._wake_all()
         self._scheduler.join()
         with self._cv:
-            self._cv.notify_all()
+            self._wake_all()
         for w in self._workers:
             w.join()
         with self._cv:
@@ -639,7 +665,13 @@ class RegridServer:
                 if not progressed:
                     self._cv.wait(timeout=0.05)
             # let the workers finish and exit
-            self._cv.notify_all()
+            self._wake_all()
+
+    def _wake_all(self) -> None:
+        """Wake the scheduler and every slot (lock held)."""
+        self._cv.notify_all()
+        for cv in self._slot_cv:
+            cv.notify_all()
 
     def _dispatch(self) -> bool:
         """Admit as many waiting requests as slots and memory allow (lock held)."""
@@ -659,7 +691,7 @@ class RegridServer:
                 for r in job.cobuild or ():
                     self._building.add(r.key)
             progressed = True
-            self._cv.notify_all()
+            self._slot_cv[slot].notify()
         return progressed
 
     def _drop_cancelled(self) -> None:
@@ -746,7 +778,7 @@ class RegridServer:
                 while self._slot_jobs[slot] is None:
                     if not self._running and not self._pending and not self._intake_n:
                         return
-                    self._cv.wait(timeout=0.05)
+                    self._slot_cv[slot].wait(timeout=0.05)
                 job = self._slot_jobs[slot]
             self._run(slot, stream, job)
 

@@ -128,25 +128,6 @@ __device__ __forceinline__ bool seg_hit(double x1, double y1, double x2, double 
     return (0 <= t && t < 1) && (0 <= u && u < 1);
 }
 
-// fl64(a - b) given d = fl64(b - a): -d unless d is a zero (whose sign
-// depends on the operands), from the bits (no FP64 instruction).
-__device__ __forceinline__ double neg_diff(double d, double a, double b) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(d);
-    if ((bits & 0x7fffffffffffffffull) == 0ull) return dsub(a, b);
-    return __longlong_as_double((long long)(bits ^ 0x8000000000000000ull));
-}
-
-// v * 0.5 as fl64(v * 0.5) gives it: for a normal v above the smallest
-// normal exponent, by decrementing the exponent field (no FP64 instruction);
-// otherwise (zero, subnormal, smallest exponent, infinity, NaN) by the
-// multiplication itself.
-__device__ __forceinline__ double half_exact(double v) {
-    const long long b = __double_as_longlong(v);
-    const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
-    if (ex > 1u && ex < 0x7ffu) return __longlong_as_double(b - (1ll << 52));
-    return dmul(v, 0.5);
-}
-
 // ---------------------------------------------------------------------------
 // Certified float32 filter for the walk's crossing test.  On GB300 the FP64
 // pipe runs 2 lanes per clock per SM (1/64 of FP32), and the 13 FP64
@@ -933,11 +914,8 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
             }
             if (found >= 0) {
                 const double t = ddiv(f_tdet, f_det);
-                // p2 - x1 is -(x1 - p2), bit for bit (rounding to nearest is
-                // symmetric), except for the sign of an exact zero: then the
-                // subtraction itself
-                x2 = dadd(x1, dmul(t, neg_diff(dx12, p2x, x1)));
-                y2 = dadd(y1, dmul(t, neg_diff(dy12, p2y, y1)));
+                x2 = dadd(x1, dmul(t, dsub(p2x, x1)));
+                y2 = dadd(y1, dmul(t, dsub(p2y, y1)));
             }
             int64_t nsy, nstx, nsty;
             if (found >= 0) {
@@ -952,7 +930,7 @@ __device__ int64_t walk_range(const SweepParams& P, const Family& F, const Stati
                 edge_last = MAXSIZE;
             }
             // _calc_and_save_weights: area_triangle, negated for axis 0
-            double area = half_exact(dsub(dmul(x1, y2), dmul(x2, y1)));
+            double area = dmul(dsub(dmul(x1, y2), dmul(x2, y1)), 0.5);
             if (F.axis == 0) area = -area;
             // when the static grid is the input grid both sides share the
             // input cell, and -area / a_in (times w_in) is exactly the

@@ -106,3 +106,38 @@ def test_budget_evicts_and_still_serves(torch):
     assert st["evictions"] > 0 and st["peak_bytes"] <= 6e6
     for (_, (gi, go), vals), got in zip(reqs, results):
         np.testing.assert_array_equal(np.asarray(got), regrid_plain(gi, go, vals).numpy())
+
+
+@pytest.mark.parametrize("accumulate", ["fast", "exact"])
+def test_large_pinned_request_is_pipelined_and_equal(torch, accumulate):
+    """A request whose stack in pinned host memory reaches the pipelining size
+    goes through rg_apply_host (chunks copied in, applied and copied out on
+    three streams); its result equals the device apply of the same weights,
+    and a batched apply of the same grid (the unpipelined path) slice for
+    slice."""
+    from regridding_gb300 import workloads
+    from regridding_gb300._device import build_conservative_2d
+    from regridding_gb300.serving import GpuBackend, RegridServer
+
+    rng = np.random.default_rng(12)
+    gi, go = workloads.grid_pair(rng, 1024)
+    n_in = (gi[0].shape[0] - 1) * (gi[0].shape[1] - 1)
+    n_out = (go[0].shape[0] - 1) * (go[0].shape[1] - 1)
+    stack = GpuBackend.PIPELINE_BYTES // (4 * n_in) + 2
+    vals = torch.empty((stack, n_in), dtype=torch.float32, pin_memory=True)
+    vals.copy_(torch.from_numpy(rng.lognormal(3, 1, (stack, n_in)).astype(np.float32)))
+    odt = torch.float32 if accumulate == "fast" else torch.float64
+    out = torch.empty((stack, n_out), dtype=odt, pin_memory=True)
+    small = vals[:2].clone()  # not pinned: the ordinary path
+    with RegridServer(hbm_budget=8e9, slots=2, accumulate=accumulate, perturb=False) as srv:
+        assert srv.backend._pipelined([type("R", (), {"values": vals, "out": out})()], None)
+        got = srv.submit(gi, go, vals, out=out).result(120)
+        got_small = srv.submit(gi, go, small).result(120)
+    dw = build_conservative_2d(gi, go)
+    try:
+        exp = dw.apply(vals.cuda(), accumulate=accumulate).cpu()
+    finally:
+        dw.free()
+    assert got.data_ptr() == out.data_ptr()
+    np.testing.assert_array_equal(got.numpy(), exp.numpy())
+    np.testing.assert_array_equal(np.asarray(got_small), exp[:2].numpy())

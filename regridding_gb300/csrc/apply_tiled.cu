@@ -839,6 +839,12 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
         }
         return;
     }
+    // The compensated apply runs every lane of a warp to the warp's longest
+    // row (a uniform bound, no divergent branch per entry).  A lane's entries
+    // past its own row have zero weights and slot 0: such a step leaves the
+    // pair (h, l) unchanged for a finite input word; a non-finite one makes
+    // the sum NaN, which sends that output and slice to the exact loop.
+    const int kwarp = MODE == MODE_FF ? __reduce_max_sync(0xffffffffu, nk) : nk;
     // PLANES: every slice of a stage has its own 4 KB plane, 1024-byte
     // aligned, so all slices see the same swizzle phase and a gather's
     // slices differ by constant offsets.  Otherwise the rows of slice q start
@@ -948,7 +954,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                 for (int j = 0; j < SPS / 2; j++) h2[j] = l2[j] = 0ull;
 #pragma unroll
                 for (int k = 0; k < CT; k++) {
-                    if (k < nk) {
+                    if (k < kwarp) {
                         const int a = li[k], b = li[k] ^ flip;
 #pragma unroll
                         for (int j = 0; j < SPS / 2; j++)
@@ -959,7 +965,7 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                 if constexpr (CT > 0) {
 #pragma unroll
                     for (int j = 0; j < NX; j++) {
-                        if (CT + j < nk) {
+                        if (CT + j < kwarp) {
                             const float wk = ex_hi[j][t], wlk = ex_lo[j][t];
                             const uint64_t kh = f2_pack(wk, wk), khn = f2_pack(-wk, -wk), kl = f2_pack(wlk, wlk);
                             const int a = ex_slot[j][t], b = a ^ flip;
@@ -988,27 +994,45 @@ __global__ void __launch_bounds__(32 * PATCH_WARPS, MINB)
                     l[2 * j] = lv.x;
                     l[2 * j + 1] = lv.y;
                 }
+                // The usual stage (every slice in range, every h and l a
+                // normal float) is tested once, with bitwise ands and a single
+                // branch, and stored without further tests (per-slice tests
+                // and branches were a measured share of the instruction
+                // stream).  Anything else takes the per-slice path.
+                bool usual = ds + SPS <= d1;
 #pragma unroll
-                for (int q = 0; q < SPS; q++) {
-                    if (ds + q >= d1) continue;
-                    double r;
-                    const unsigned uh = __float_as_uint(h[q]), ul = __float_as_uint(l[q]);
-                    if (normal_bits(uh) && normal_bits(ul)) {
-                        r = __dadd_rn(widen_normal(uh), widen_normal(ul));
-                    } else if (nk == 0) {
-                        r = 0.0;
-                    } else if (finite_bits(h[q]) && finite_bits(l[q])) {
-                        r = __dadd_rn(widen(h[q]), widen(l[q]));
-                    } else {
-                        // a float32 partial sum overflowed, or an input or a
-                        // weight is not finite: this output and slice in
-                        // float64, stored order (the exact apply's sum)
-                        r = 0.0;
-                        for (int64_t k = s; k < e; k++)
-                            r = __dadd_rn(r, __dmul_rn(dval[k], widen(buf[q * plane + (box_slot_of(col[k], org, nd) ^
-                                                                                     ((q & 1) ? flip : 0))])));
+                for (int q = 0; q < SPS; q++)
+                    usual = usual & normal_bits(__float_as_uint(h[q])) & normal_bits(__float_as_uint(l[q]));
+                if (usual) {
+                    double* dst = vout64 + ds * n_out + o;
+#pragma unroll
+                    for (int q = 0; q < SPS; q++)
+                        dst[q * n_out] =
+                            __dadd_rn(widen_normal(__float_as_uint(h[q])), widen_normal(__float_as_uint(l[q])));
+                } else {
+#pragma unroll
+                    for (int q = 0; q < SPS; q++) {
+                        if (ds + q >= d1) continue;
+                        double r;
+                        const unsigned uh = __float_as_uint(h[q]), ul = __float_as_uint(l[q]);
+                        if (normal_bits(uh) && normal_bits(ul)) {
+                            r = __dadd_rn(widen_normal(uh), widen_normal(ul));
+                        } else if (nk == 0) {
+                            r = 0.0;
+                        } else if (finite_bits(h[q]) && finite_bits(l[q])) {
+                            r = __dadd_rn(widen(h[q]), widen(l[q]));
+                        } else {
+                            // a float32 partial sum overflowed, or an input or
+                            // a weight is not finite (or a padded step read a
+                            // non-finite word): this output and slice in
+                            // float64, stored order (the exact apply's sum)
+                            r = 0.0;
+                            for (int64_t k = s; k < e; k++)
+                                r = __dadd_rn(r, __dmul_rn(dval[k], widen(buf[q * plane + (box_slot_of(col[k], org, nd) ^
+                                                                                         ((q & 1) ? flip : 0))])));
+                        }
+                        vout64[(ds + q) * n_out + o] = r;
                     }
-                    vout64[(ds + q) * n_out + o] = r;
                 }
             }
         } else if (o >= 0) {
@@ -1585,7 +1609,7 @@ constexpr int kNumBoxConfigs = (int)(sizeof(kBoxConfigs) / sizeof(kBoxConfigs[0]
 struct FFConfig {
     int sps, nst, minb, cached;
 };
-constexpr FFConfig kFFConfigs[] = {{4, 2, 0, 6}, {4, 2, 0, 7}, {4, 3, 0, 6}, {8, 2, 0, 6},
+constexpr FFConfig kFFConfigs[] = {{6, 2, 0, 6}, {8, 2, 0, 6}, {4, 2, 0, 6}, {4, 3, 0, 6},
                                    {2, 4, 0, 6}, {4, 3, 3, 4}, {4, 2, 4, 0}};
 constexpr int kNumFFConfigs = (int)(sizeof(kFFConfigs) / sizeof(kFFConfigs[0]));
 
@@ -1666,10 +1690,10 @@ int launch_ff_config(const rg_weights_s* W, int cfg, const float* vin, void* vou
     CUtensorMap map;
     if (!encode_stack(W, vin, stack, 1, &map)) return RG_ERR_UNSUPPORTED;
     switch (cfg) {
-        case 0: return launch_patch<4, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
-        case 1: return launch_patch<4, 2, 0, MODE_FF, 7>(W, map, bs, vin, vout, stack, s);
-        case 2: return launch_patch<4, 3, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
-        case 3: return launch_patch<8, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 0: return launch_patch<6, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 1: return launch_patch<8, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 2: return launch_patch<4, 2, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
+        case 3: return launch_patch<4, 3, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
         case 4: return launch_patch<2, 4, 0, MODE_FF, 6>(W, map, bs, vin, vout, stack, s);
         case 5: return launch_patch<4, 3, 3, MODE_FF, 4>(W, map, bs, vin, vout, stack, s);
         case 6: return launch_patch<4, 2, 4, MODE_FF, 0>(W, map, bs, vin, vout, stack, s);

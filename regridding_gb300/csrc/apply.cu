@@ -221,12 +221,12 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
         if (tiled && box_usable(W, (const float*)vin, stack)) {
             RG_TRY(box_lists_for(W, s, &made));
             use_box = W->box_state == 1;
-            if (use_box && W->box_cfg == -1) {
+            if (use_box && W->box_cfg[stack_class(stack)] == -1) {
                 if (made) RG_CUDA(cudaStreamSynchronize(s));
                 made = false;
                 RG_TRY(tune_box_fast(W, (const float*)vin, (float*)vout, stack, s));
             }
-            use_box = use_box && W->box_cfg >= 0;
+            use_box = use_box && W->box_cfg[stack_class(stack)] >= 0;
         }
         if (exact_box && box_usable(W, (const float*)vin, stack)) {
             RG_TRY(box_lists_for(W, s, &made));
@@ -237,12 +237,12 @@ int apply_weights(rg_weights_s* W, bool transposed, const void* vin, int dtype_i
             RG_TRY(box_lists_for(W, s, &made));
             use_box_ff = W->box_state == 1;
             if (use_box_ff) RG_TRY(ff_lists_for(W, s, &made));
-            if (use_box_ff && W->box_cfg_ff == -1) {
+            if (use_box_ff && W->box_cfg_ff[stack_class(stack)] == -1) {
                 if (made) RG_CUDA(cudaStreamSynchronize(s));
                 made = false;
                 RG_TRY(tune_box_ff(W, (const float*)vin, (double*)vout, stack, s));
             }
-            use_box_ff = use_box_ff && W->box_cfg_ff >= 0;
+            use_box_ff = use_box_ff && W->box_cfg_ff[stack_class(stack)] >= 0;
         }
         if (tiled && !use_box) RG_TRY(rows_usable(W, (const float*)vin, stack, s, &made, &use_rows));
         if (tiled && !use_box && !use_rows) RG_TRY(tiled_lists_for(W, (const float*)vin, s, &g, &made));

@@ -1729,24 +1729,18 @@ int forced_box_config(int mode) {
     return -1;
 }
 
-// Autotuner: on the first TMA apply of a handle, time every configuration
-// on the real call (each run writes the same result) and keep the fastest;
-// later handles of the same kind (box height, stack size class) reuse the
-// choice without timing.  The caller holds the handle's lock; synchronises
+// Autotuner: on the first TMA apply of a handle in a stack size class, time
+// every configuration on the real call (each run writes the same result) and
+// keep the fastest for that class; later handles of the same kind (box
+// height, stack size class) reuse the choice without timing.  The caller holds the handle's lock; synchronises
 // the stream.
 // Tuned configurations shared by handles of the same kind: box height and
 // stack size class (1, 2-3, 4-7, ..., 64+) -> configuration.
 std::mutex g_tuned_mutex;
 std::map<std::tuple<int, int, int>, int> g_tuned;  // (mode, box rows, stack class) -> configuration
 
-int stack_class(int64_t stack) {
-    int c = 0;
-    while (c < 6 && ((int64_t)2 << c) <= stack) c++;
-    return c;
-}
-
 int tune_box(rg_weights_s* W, int mode, const float* vin, void* vout, int64_t stack, cudaStream_t s) {
-    int& chosen = mode == MODE_FF ? W->box_cfg_ff : W->box_cfg;
+    int& chosen = (mode == MODE_FF ? W->box_cfg_ff : W->box_cfg)[stack_class(stack)];
     if (chosen >= 0) return RG_OK;
     const int forced = forced_box_config(mode);
     if (forced >= 0) {
@@ -1812,14 +1806,16 @@ int tune_box(rg_weights_s* W, int mode, const float* vin, void* vout, int64_t st
 // the tuned configuration does not take this call, so the caller can take
 // another kernel.
 int apply_box(const rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {
-    if (W->box_cfg < 0) return RG_ERR_UNSUPPORTED;
-    return launch_box_config(W, MODE_FAST, W->box_cfg, vin, vout, stack, s);
+    const int cfg = W->box_cfg[stack_class(stack)];
+    if (cfg < 0) return RG_ERR_UNSUPPORTED;
+    return launch_box_config(W, MODE_FAST, cfg, vin, vout, stack, s);
 }
 
 // The compensated (float-float) TMA apply with its tuned configuration.
 int apply_box_ff(const rg_weights_s* W, const float* vin, double* vout, int64_t stack, cudaStream_t s) {
-    if (W->box_state != 1 || W->box_cfg_ff < 0 || !W->ff_slot || !W->ff_perm) return RG_ERR_UNSUPPORTED;
-    return launch_box_config(W, MODE_FF, W->box_cfg_ff, vin, vout, stack, s);
+    const int cfg = W->box_cfg_ff[stack_class(stack)];
+    if (W->box_state != 1 || cfg < 0 || !W->ff_slot || !W->ff_perm) return RG_ERR_UNSUPPORTED;
+    return launch_box_config(W, MODE_FF, cfg, vin, vout, stack, s);
 }
 
 int tune_box_fast(rg_weights_s* W, const float* vin, float* vout, int64_t stack, cudaStream_t s) {

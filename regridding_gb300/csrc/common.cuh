@@ -191,6 +191,17 @@ int bucket_sort(const int32_t* bucket, const int64_t* skey, int64_t n, int64_t n
                 int64_t* bucket_ptr, uint32_t* perm, unsigned* flags, cudaStream_t s,
                 const double* val = nullptr, int32_t* out_hi = nullptr, double* out_val = nullptr);
 
+// Stack size classes of the apply autotuner (1, 2-3, 4-7, ..., 32-63, 64 and
+// more slices).  A handle keeps one tuned configuration per class: the best
+// number of slices per stage depends on how many slices a call has (a stage
+// computes all its slices, also those past the end of the stack).
+constexpr int kStackClasses = 7;
+inline int stack_class(int64_t stack) {
+    int c = 0;
+    while (c < kStackClasses - 1 && ((int64_t)2 << c) <= stack) c++;
+    return c;
+}
+
 }  // namespace rg
 
 // Opaque weight matrix of one orthogonal element, resident on the device.
@@ -226,7 +237,8 @@ struct rg_weights_s {
     int box_state = 0;  // 0 not built, 1 ready, -1 not applicable
     int box_rows = 0, box_cols = 0;
     int64_t box_patches = 0;
-    int box_cfg = -1;  // configuration chosen by the autotuner (-1 not tuned, -2 none fits)
+    // configuration chosen by the autotuner per stack class (-1 not tuned, -2 none fits)
+    int box_cfg[rg::kStackClasses] = {-1, -1, -1, -1, -1, -1, -1};
     int2* box_origin = nullptr;
     uint16_t* box_slot = nullptr;  // per entry, in the order the TMA kernel gathers them
     uint8_t* box_perm = nullptr;   // exact apply: per patch, thread -> output (longest rows first)
@@ -238,7 +250,7 @@ struct rg_weights_s {
     uint16_t* ff_slot = nullptr;
     float* ff_hi = nullptr;
     float* ff_lo = nullptr;
-    int box_cfg_ff = -1;
+    int box_cfg_ff[rg::kStackClasses] = {-1, -1, -1, -1, -1, -1, -1};
     unsigned* dflags = nullptr;  // device error word of the asynchronous (TMA) apply
     int rows_maxlen = -1;        // longest row (for the row kernel; -1 not known yet)
     int device = 0;

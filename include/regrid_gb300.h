@@ -165,8 +165,13 @@ int rg_weights_free(rg_weights w, rg_stream_t stream);
  * float64 result bit for bit (dtype_out must be RG_F64, or RG_F32 for the
  * upstream in-place float32 output, which rounds after every update);
  * RG_ACC_FAST accumulates in dtype_out with FMA; RG_ACC_COMPENSATED gives a
- * float64 result within 1e-12 of the upstream's for float32 input, about 4x
- * faster than RG_ACC_EXACT on GB300 (see its definition above). */
+ * float64 result within 1e-12 of the upstream's for float32 input, about 5x
+ * faster than RG_ACC_EXACT on GB300 (see its definition above).
+ * The first fast or compensated apply of a handle (which builds its tile
+ * lists and entry orders) and its first in each stack size class (1, 2-3,
+ * 4-7, ..., 64 and more slices: the autotuner times its configurations on
+ * that call, unless an earlier handle of the same kind was tuned) synchronise
+ * `stream`; later applies are asynchronous. */
 int rg_apply(rg_weights w, const void* d_vin, int dtype_in, void* d_vout, int dtype_out,
              int64_t stack, int acc, rg_stream_t stream);
 

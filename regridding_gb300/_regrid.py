@@ -58,8 +58,8 @@ def regrid_from_weights(
     otherwise): the HBM-bandwidth path, within about 1e-6 relative of the
     float64 result.  ``accumulate="compensated"`` returns the upstream's
     float64 output within 1e-12 relative of it, computed for float32 input
-    in float-float arithmetic on the FP32 pipe, about 4x faster than
-    ``"exact"`` (other inputs compute as ``"exact"``).
+    in float-float arithmetic on the FP32 pipe, about 5x faster than
+    ``"exact"`` on GB300 (other inputs compute as ``"exact"``).
     """
     if accumulate not in ("exact", "fast", "compensated"):
         raise ValueError(f"accumulate must be 'exact', 'fast' or 'compensated', got {accumulate!r}")
